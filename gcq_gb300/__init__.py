@@ -1,0 +1,233 @@
+"""gcq_gb300: gCQ's GPU concurrent FIFO queues (G-WFQ, G-LFQ, WFQ-YMC, SFQ) on GB300.
+
+The product is the CUDA code in include/gcq/*.cuh and gcq_gb300/csrc/*.cu, built
+for sm_103a into gcq_gb300/_build/libgcq.so with the C ABI of include/gcq.h.  This
+module is a thin ctypes binding to that library for Python callers, the tests and
+bench.py.  There is no CPU fallback: if libgcq.so is missing, or no CUDA device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgcq.so")
+
+KINDS = {"gwfq": 0, "glfq": 1, "wfq": 2, "sfq": 3}
+KIND_NAMES = {v: k for k, v in KINDS.items()}
+
+# gcq_status
+OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, EDEVICE, EUNSUPPORTED, ECAPACITY = 0, -1, -2, -3, -4, -5, -6, -7
+ERR_SPIN, ERR_TIMEOUT, ERR_TID, ERR_POOL, ERR_CAPACITY = 0x1, 0x2, 0x4, 0x8, 0x10
+
+# gcq_log_entry (include/gcq.h)
+LOG_DTYPE = np.dtype([("proc", "<u8"), ("op", "<u4"), ("_pad", "<u4"), ("arg", "<u8"),
+                      ("ret", "<u8"), ("call", "<i8"), ("end", "<i8")])
+
+
+class Knobs(C.Structure):
+    _fields_ = [("help_delay", C.c_uint32), ("enq_patience", C.c_uint32), ("deq_patience", C.c_uint32),
+                ("remap", C.c_uint32), ("ymc_patience", C.c_uint32), ("ymc_ops_per_thread", C.c_uint32),
+                ("wait_timeout_ns", C.c_uint64)]
+
+
+class TbCounters(C.Structure):
+    _fields_ = [("enq_success", C.c_uint64), ("enq_fail", C.c_uint64),
+                ("deq_success", C.c_uint64), ("deq_empty", C.c_uint64)]
+
+
+class TbResult(C.Structure):
+    _fields_ = [("counters", TbCounters), ("gpu_ms", C.c_double), ("launches", C.c_uint64)]
+
+
+class FifoResult(C.Structure):
+    _fields_ = [("in_count", C.c_uint64), ("out_count", C.c_uint64), ("err_oob", C.c_uint32),
+                ("err_dup", C.c_uint32), ("err_order", C.c_uint32), ("err_missing", C.c_uint32),
+                ("err_gt1", C.c_uint32), ("ops_per_thread", C.c_uint32), ("verified", C.c_int),
+                ("_pad", C.c_int)]
+
+
+class GcqError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = "%s: %s" % (what, _lib().gcq_strerror(status).decode()) if _LIB else str(status)
+        if status == ECUDA and _LIB:
+            msg += " (%s)" % _lib().gcq_last_cuda_error().decode()
+        super().__init__(msg)
+
+
+# Exported symbols with (argtypes, restype); the CPU tests check that each one is
+# present in libgcq.so and declared in include/gcq.h.
+P, U32, U64, I32, SZ = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_size_t
+SIGNATURES = {
+    "gcq_default_knobs": ([C.POINTER(Knobs)], None),
+    "gcq_create": ([I32, U32, U32, C.POINTER(Knobs), C.POINTER(P)], I32),
+    "gcq_destroy": ([P], I32),
+    "gcq_reset": ([P, P], I32),
+    "gcq_device_ptr": ([P, C.POINTER(P)], I32),
+    "gcq_error_word": ([P, C.POINTER(U32), I32], I32),
+    "gcq_device_bytes": ([P], U64),
+    "gcq_info": ([P, C.POINTER(I32), C.POINTER(U32), C.POINTER(U32)], I32),
+    "gcq_strerror": ([I32], C.c_char_p),
+    "gcq_last_cuda_error": ([], C.c_char_p),
+    "gcq_run_history": ([P, U32, U32, U32, I32, I32, I32, P, SZ, C.POINTER(SZ), P], I32),
+    "gcq_tb_launch": ([P, I32, I32, U32, U32, U32, U64, P, P], I32),
+    "gcq_tb_chunk_host": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
+    "gcq_tb_run": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
+    "gcq_fifo_check": ([P, U32, U32, U32, C.POINTER(FifoResult)], I32),
+}
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgcq.so is not built (%s); run __graft_entry__.build() or "
+                               "python -m gcq_gb300.build" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.argtypes = args
+            f.restype = res
+        _LIB = L
+    return _LIB
+
+
+def lib():
+    """The loaded libgcq.so (ctypes.CDLL)."""
+    return _lib()
+
+
+def _check(rc, what):
+    if rc != OK:
+        raise GcqError(rc, what)
+
+
+def default_knobs() -> Knobs:
+    k = Knobs()
+    _lib().gcq_default_knobs(C.byref(k))
+    return k
+
+
+class Queue:
+    """One device queue owned by libgcq.so (gcq_create / gcq_destroy)."""
+
+    def __init__(self, kind: str, capacity_log2: int, max_threads: int, knobs: Knobs | None = None,
+                 **overrides):
+        if kind not in KINDS:
+            raise ValueError("kind must be one of %s" % sorted(KINDS))
+        k = knobs or default_knobs()
+        for name, v in overrides.items():
+            setattr(k, name, v)
+        h = P()
+        _check(_lib().gcq_create(KINDS[kind], capacity_log2, max_threads, C.byref(k), C.byref(h)),
+               "gcq_create(%s, 2^%d, %d)" % (kind, capacity_log2, max_threads))
+        self._h = h
+        self.kind = kind
+        self.capacity_log2 = capacity_log2
+        self.max_threads = max_threads
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            _lib().gcq_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self, stream: int = 0):
+        _check(_lib().gcq_reset(self._h, P(stream)), "gcq_reset")
+
+    def device_ptr(self) -> int:
+        d = P()
+        _check(_lib().gcq_device_ptr(self._h, C.byref(d)), "gcq_device_ptr")
+        return d.value
+
+    def device_bytes(self) -> int:
+        return int(_lib().gcq_device_bytes(self._h))
+
+    def error_word(self, clear: bool = False) -> int:
+        e = U32()
+        _check(_lib().gcq_error_word(self._h, C.byref(e), int(clear)), "gcq_error_word")
+        return e.value
+
+    # --- history harness -------------------------------------------------------
+    def history(self, threads: int, ops: int, block: int = 256, mode: int = 0, producer_percent: int = 50,
+                value_mode: int = 0, stream: int = 0) -> np.ndarray:
+        cap = threads * ops * 2
+        out = np.zeros(cap, dtype=LOG_DTYPE)
+        n = SZ()
+        _check(_lib().gcq_run_history(self._h, threads, block, ops, mode, producer_percent, value_mode,
+                                      out.ctypes.data, cap, C.byref(n), P(stream)), "gcq_run_history")
+        return out[: n.value].copy()
+
+    # --- throughput harness ----------------------------------------------------
+    def tb_launch(self, mode: int, threads: int, chunk_ops: int, dev_counters: int, block: int = 256,
+                  producer_percent: int = 50, seed: int = 0, stream: int = 0):
+        _check(_lib().gcq_tb_launch(self._h, mode, producer_percent, threads, block, chunk_ops, seed,
+                                    P(dev_counters), P(stream)), "gcq_tb_launch")
+
+    def tb_chunk_host(self, mode: int, threads: int, chunk_ops: int, payloads: np.ndarray, block: int = 256,
+                      producer_percent: int = 50, stream: int = 0) -> dict:
+        assert payloads.dtype == np.uint32 and payloads.size == threads * chunk_ops
+        c = TbCounters()
+        _check(_lib().gcq_tb_chunk_host(self._h, mode, producer_percent, threads, block, chunk_ops,
+                                        payloads.ctypes.data, C.byref(c), P(stream)), "gcq_tb_chunk_host")
+        return {f: getattr(c, f) for f, _ in TbCounters._fields_}
+
+    def tb_run(self, mode: int, threads: int, chunk_ops: int = 128, block: int = 256, producer_percent: int = 50,
+               warmup_ms: float = 200.0, run_ms: float = 1000.0, graph_chunks: int = 16) -> dict:
+        r = TbResult()
+        _check(_lib().gcq_tb_run(self._h, mode, producer_percent, threads, block, chunk_ops, warmup_ms, run_ms,
+                                 graph_chunks, C.byref(r)), "gcq_tb_run")
+        c = r.counters
+        sec = r.gpu_ms / 1e3
+        d = {f: getattr(c, f) for f, _ in TbCounters._fields_}
+        d.update(gpu_ms=r.gpu_ms, launches=r.launches,
+                 succ_mops=(c.enq_success + c.deq_success) / sec / 1e6 if sec > 0 else 0.0,
+                 enq_mops=c.enq_success / sec / 1e6 if sec > 0 else 0.0,
+                 deq_mops=c.deq_success / sec / 1e6 if sec > 0 else 0.0,
+                 empty_mops=c.deq_empty / sec / 1e6 if sec > 0 else 0.0,
+                 fail_mops=c.enq_fail / sec / 1e6 if sec > 0 else 0.0)
+        return d
+
+    # --- FIFO check --------------------------------------------------------------
+    def fifo_check(self, threads: int, ops_per_thread: int = 32, block: int = 256) -> dict:
+        r = FifoResult()
+        _check(_lib().gcq_fifo_check(self._h, threads, block, ops_per_thread, C.byref(r)), "gcq_fifo_check")
+        return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+
+def history_to_jsonl(recs: np.ndarray, path: str, reference_format: bool = False):
+    """Write records as the reference's JSONL (correctness/history.cpp:271-280).
+
+    reference_format=True writes a failed-without-effect dequeue (op 2) as the
+    reference does, op 1 with ret 0.
+    """
+    with open(path, "w") as f:
+        for r in recs:
+            op = int(r["op"])
+            if reference_format and op == 2:
+                op = 1
+            f.write('{"proc":%d,"op":%d,"arg":%d,"ret":%d,"call":%d,"end":%d}\n'
+                    % (r["proc"], op, r["arg"], r["ret"], r["call"], r["end"]))

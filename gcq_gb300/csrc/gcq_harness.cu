@@ -1,0 +1,476 @@
+// Harness kernels of libgcq.so: history recording (correctness/history.cpp),
+// fixed-duration throughput chunks (throughout_bench.cpp) and the produce-then-drain
+// FIFO check (throughout_bench.cpp MODE_FIFO), for all four queues.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "gcq_internal.cuh"
+
+using gcqi::qops;
+
+namespace {
+
+// ------------------------------------------------------------------ helpers
+template <int K>
+__device__ __forceinline__ typename qops<K>::Q* as_q(void* p) {
+    return reinterpret_cast<typename qops<K>::Q*>(p);
+}
+
+// Sum four per-thread counters over the block and add them to `out` with one
+// atomic per counter per block (the reference adds per thread, :836-839).
+__device__ __forceinline__ void block_add_counters(uint64_t a, uint64_t b, uint64_t c, uint64_t d,
+                                                   gcq_tb_counters* out) {
+    __shared__ unsigned long long s[4][32];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned nwarps = (blockDim.x + 31) >> 5;
+    unsigned long long v[4] = {a, b, c, d};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+        for (int k = 0; k < 4; ++k) s[k][warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            unsigned long long x = lane < nwarps ? s[k][lane] : 0ull;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            v[k] = x;
+        }
+        if (lane == 0) {
+            unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+            if (v[0]) atomicAdd(&o[0], v[0]);
+            if (v[1]) atomicAdd(&o[1], v[1]);
+            if (v[2]) atomicAdd(&o[2], v[2]);
+            if (v[3]) atomicAdd(&o[3], v[3]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ throughput
+// balanced_chunk_kernel (mode 0, throughout_bench.cpp:810-840) and
+// split_chunk_kernel (mode 1, :842-882) in one body.  Payload i of thread t is
+// payloads[i * threads + t] when payloads is given, else splitmix64(seed, t, i).
+// All lanes stay to the end for the block reduction (the reference returns early).
+template <int K>
+__global__ void __launch_bounds__(1024) k_tb_chunk(void* qv, int mode, int producer_percent, uint32_t threads,
+                                                   uint32_t chunk_ops, uint64_t seed, const uint32_t* payloads,
+                                                   gcq_tb_counters* ctr) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t eo = 0, ef = 0, dok = 0, de = 0;
+    if (tid < threads) {
+        const bool producer = ((uint64_t)tid * 100u / threads) < (uint64_t)producer_percent;
+        const bool nb = (mode == 1);   // SFQ: blocking when balanced, non-blocking when split
+        for (uint32_t i = 0; i < chunk_ops; ++i) {
+            if (mode == 0 || producer) {
+                const uint32_t p = payloads ? payloads[(uint64_t)i * threads + tid]
+                                            : (uint32_t)gcqi::splitmix64(seed ^ (((uint64_t)tid << 32) | i));
+                if (qops<K>::enq(q, qops<K>::tb_value(p), tid, nb)) ++eo; else ++ef;
+            }
+            if (mode == 0 || !producer) {
+                uint64_t out = 0;
+                if (qops<K>::deq(q, &out, tid, nb) == 1) ++dok; else ++de;
+            }
+        }
+    }
+    block_add_counters(eo, ef, dok, de, ctr);
+}
+
+const void* tb_kernel(int kind) {
+    switch (kind) {
+        case GCQ_GWFQ: return (const void*)k_tb_chunk<GCQ_GWFQ>;
+        case GCQ_GLFQ: return (const void*)k_tb_chunk<GCQ_GLFQ>;
+        case GCQ_WFQ: return (const void*)k_tb_chunk<GCQ_WFQ>;
+        case GCQ_SFQ: return (const void*)k_tb_chunk<GCQ_SFQ>;
+    }
+    return nullptr;
+}
+
+int check_tb_args(gcq_queue* q, int mode, int pct, uint32_t threads, uint32_t block, uint32_t chunk_ops) {
+    if (!q || threads == 0 || block == 0 || block > 1024 || (block & 31) || chunk_ops == 0) return GCQ_EINVAL;
+    if (mode != 0 && mode != 1) return GCQ_EINVAL;
+    if (mode == 1 && (pct < 0 || pct > 100)) return GCQ_EINVAL;
+    if (threads > q->max_threads) return GCQ_EINVAL;
+    if (q->kind == GCQ_SFQ && mode == 0) {
+        // blocking SFQ waits on other threads: all of them must be resident
+        uint64_t res = 0;
+        int rc = gcqi::resident_threads(tb_kernel(q->kind), (int)block, 0, &res);
+        if (rc != GCQ_OK) return rc;
+        if (threads > res) return GCQ_EUNSUPPORTED;
+    }
+    return GCQ_OK;
+}
+
+int launch_tb(gcq_queue* q, int mode, int pct, uint32_t threads, uint32_t block, uint32_t chunk_ops,
+              uint64_t seed, const uint32_t* payloads, gcq_tb_counters* ctr, cudaStream_t s) {
+    const unsigned grid = (threads + block - 1) / block;
+    switch (q->kind) {
+        case GCQ_GWFQ: k_tb_chunk<GCQ_GWFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
+        case GCQ_GLFQ: k_tb_chunk<GCQ_GLFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
+        case GCQ_WFQ: k_tb_chunk<GCQ_WFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
+        case GCQ_SFQ: k_tb_chunk<GCQ_SFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
+        default: return GCQ_EINVAL;
+    }
+    GCQ_CUDA(cudaGetLastError());
+    return GCQ_OK;
+}
+
+int read_error_word(gcq_queue* q, cudaStream_t s, uint32_t* err) {
+    GCQ_CUDA(cudaMemcpyAsync(err, q->err, 4, cudaMemcpyDeviceToHost, s));
+    GCQ_CUDA(cudaStreamSynchronize(s));
+    return GCQ_OK;
+}
+
+// Map the error word after a harness run: timeouts and bounded loops are errors;
+// YMC pool exhaustion is the reference's documented behaviour (failed operations).
+int status_of(uint32_t err) {
+    if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
+    if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID | GCQ_ERR_CAPACITY)) return GCQ_EDEVICE;
+    return GCQ_OK;
+}
+
+// ------------------------------------------------------------------ history
+// alternating_history_kernel / split_history_kernel (history.cpp:188-227) with the
+// WF_LOG_* bracketing of wf_linlog.hpp:25-45.  The clock RMWs are acq_rel, so a
+// record whose end precedes another's call happens before it.
+__device__ __forceinline__ uint64_t hist_value(int kind, int value_mode, uint32_t tid, uint32_t seq) {
+    if (kind == GCQ_SFQ) return (uint64_t)(((tid & 0x7FFFu) << 16) | ((seq + 1u) & 0xFFFFu));
+    if (value_mode == 1) return (uint64_t)(((tid & 0xFFFFu) << 16) | ((seq + 1u) & 0xFFFFu));
+    return ((uint64_t)tid << 32) | (uint64_t)(seq + 1u);
+}
+
+template <int K>
+__global__ void k_history(void* qv, uint32_t threads, uint32_t ops, int mode, int pct, int value_mode,
+                          gcq_log_entry* log, uint32_t stride, gcq::u64a* clock) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= threads) return;
+    const bool producer = ((uint64_t)tid * 100u / threads) < (uint64_t)pct;
+    gcq_log_entry* my = log + (uint64_t)tid * stride;
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < ops; ++i) {
+        if (mode == 0 || producer) {
+            const uint64_t v = hist_value(K, value_mode, tid, i);
+            gcq_log_entry* e = &my[k++];
+            e->proc = tid; e->op = 0; e->arg = v;
+            e->call = (int64_t)gcq::fetch_add(clock, 1ull);
+            const bool ok = qops<K>::enq(q, v, tid, true);
+            e->ret = ok ? 1 : 0;
+            e->end = (int64_t)gcq::fetch_add(clock, 1ull);
+        }
+        if (mode == 0 || !producer) {
+            gcq_log_entry* e = &my[k++];
+            e->proc = tid; e->op = 1; e->arg = 0;
+            e->call = (int64_t)gcq::fetch_add(clock, 1ull);
+            uint64_t out = 0;
+            const int r = qops<K>::deq(q, &out, tid, true);
+            e->ret = (r == 1) ? out : 0;
+            if (r == 2) e->op = 2;   // failed without effect (SFQ BUSY)
+            e->end = (int64_t)gcq::fetch_add(clock, 1ull);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ FIFO check
+__device__ __forceinline__ uint64_t fifo_token(int kind, uint32_t tid, uint32_t seq) {
+    if (kind == GCQ_SFQ) return (uint64_t)(((tid & 0x7FFFu) << 16) | ((seq + 1u) & 0xFFFFu));
+    return ((uint64_t)tid << 32) | (uint64_t)(seq + 1u);
+}
+
+// fifo_produce_kernel, throughout_bench.cpp:531-542, with a deadline per token.
+template <int K>
+__global__ void k_fifo_produce(void* qv, uint32_t threads, uint32_t ops, uint64_t timeout_ns, gcq::u32a* err) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= threads) return;
+    for (uint32_t i = 0; i < ops; ++i) {
+        const uint64_t tok = fifo_token(K, tid, i);
+        gcq::backoff bo;
+        const uint64_t t0 = gcq::globaltimer_ns();
+        while (!qops<K>::enq(q, tok, tid, true)) {
+            if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+            bo.pause(512);
+        }
+    }
+}
+
+// fifo_drain_kernel, throughout_bench.cpp:544-590.  Each taken token records its
+// dequeue's (call, end) on the logical clock for the order check on the host.
+template <int K>
+__global__ void k_fifo_drain(void* qv, uint32_t threads, uint32_t ops, uint64_t total, uint32_t* counts,
+                             int64_t* calls, int64_t* ends, gcq::u64a* consumed, gcq::u64a* clock,
+                             gcq::u32a* oob, uint64_t timeout_ns, gcq::u32a* err) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= threads) return;
+    gcq::backoff bo;
+    uint64_t t0 = gcq::globaltimer_ns();
+    while (gcq::ld_acq(consumed) < total) {
+        const int64_t c0 = (int64_t)gcq::fetch_add(clock, 1ull);
+        uint64_t v = 0;
+        const int r = qops<K>::deq(q, &v, tid, true);
+        const int64_t c1 = (int64_t)gcq::fetch_add(clock, 1ull);
+        if (r != 1) {
+            if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+            bo.pause(512);
+            continue;
+        }
+        bo = gcq::backoff();
+        t0 = gcq::globaltimer_ns();
+        if (gcq::fetch_add(consumed, 1ull) >= total) continue;
+        uint32_t ptid, seq;
+        if (K == GCQ_SFQ) { ptid = (uint32_t)(v >> 16) & 0x7FFFu; seq = ((uint32_t)v & 0xFFFFu) - 1u; }
+        else { ptid = (uint32_t)(v >> 32); seq = (uint32_t)v - 1u; }
+        if (ptid >= threads || seq >= ops) { atomicAdd(oob, 1u); continue; }
+        const uint64_t slot = (uint64_t)ptid * ops + seq;
+        if (atomicAdd(&counts[slot], 1u) == 0u) {
+            calls[slot] = c0;
+            ends[slot] = c1;
+        }
+    }
+}
+
+template <typename F>
+int dispatch(int kind, F&& f) {
+    switch (kind) {
+        case GCQ_GWFQ: return f(std::integral_constant<int, GCQ_GWFQ>());
+        case GCQ_GLFQ: return f(std::integral_constant<int, GCQ_GLFQ>());
+        case GCQ_WFQ: return f(std::integral_constant<int, GCQ_WFQ>());
+        case GCQ_SFQ: return f(std::integral_constant<int, GCQ_SFQ>());
+    }
+    return GCQ_EINVAL;
+}
+
+// RAII device buffer
+struct dbuf {
+    void* p = nullptr;
+    ~dbuf() { if (p) cudaFree(p); }
+    cudaError_t alloc(size_t n) { return cudaMalloc(&p, n); }
+};
+
+}  // namespace
+
+extern "C" {
+
+int gcq_tb_launch(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                  uint32_t chunk_ops, uint64_t seed, void* dev_counters, void* stream) {
+    int rc = check_tb_args(q, mode, producer_percent, threads, block, chunk_ops);
+    if (rc != GCQ_OK) return rc;
+    if (!dev_counters) return GCQ_EINVAL;
+    return launch_tb(q, mode, producer_percent, threads, block, chunk_ops, seed, nullptr,
+                     (gcq_tb_counters*)dev_counters, gcqi::as_stream(stream));
+}
+
+int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                      uint32_t chunk_ops, const uint32_t* host_payloads, gcq_tb_counters* host_counters,
+                      void* stream) {
+    int rc = check_tb_args(q, mode, producer_percent, threads, block, chunk_ops);
+    if (rc != GCQ_OK) return rc;
+    if (!host_payloads || !host_counters) return GCQ_EINVAL;
+    cudaStream_t s = gcqi::as_stream(stream);
+    // device staging: payloads + counters, kept across calls of the same size
+    static thread_local void* stage = nullptr;
+    static thread_local size_t stage_bytes = 0;
+    const size_t pbytes = (size_t)threads * chunk_ops * sizeof(uint32_t);
+    const size_t need = pbytes + 256;
+    if (stage_bytes < need) {
+        if (stage) cudaFree(stage);
+        stage = nullptr;
+        stage_bytes = 0;
+        GCQ_CUDA(cudaMalloc(&stage, need));
+        stage_bytes = need;
+    }
+    uint32_t* d_pay = (uint32_t*)stage;
+    gcq_tb_counters* d_ctr = (gcq_tb_counters*)((char*)stage + ((pbytes + 127) / 128) * 128);
+    GCQ_CUDA(cudaMemcpyAsync(d_pay, host_payloads, pbytes, cudaMemcpyHostToDevice, s));
+    GCQ_CUDA(cudaMemsetAsync(d_ctr, 0, sizeof(gcq_tb_counters), s));
+    rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, d_pay, d_ctr, s);
+    if (rc != GCQ_OK) return rc;
+    GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
+    GCQ_CUDA(cudaStreamSynchronize(s));
+    return GCQ_OK;
+}
+
+int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+               uint32_t chunk_ops, double warmup_ms, double run_ms, uint32_t graph_chunks,
+               gcq_tb_result* out) {
+    int rc = check_tb_args(q, mode, producer_percent, threads, block, chunk_ops);
+    if (rc != GCQ_OK) return rc;
+    if (!out || graph_chunks == 0) return GCQ_EINVAL;
+    memset(out, 0, sizeof(*out));
+    cudaStream_t s;
+    GCQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    dbuf ctr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaStreamDestroy(s);
+    };
+    auto fail = [&](int r) { cleanup(); return r; };
+    if (ctr.alloc(sizeof(gcq_tb_counters)) != cudaSuccess) return fail(GCQ_ENOMEM);
+    gcq_tb_counters* d_ctr = (gcq_tb_counters*)ctr.p;
+    // capture graph_chunks chunk launches (distinct payload seeds) as one graph
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fail(GCQ_ECUDA);
+    for (uint32_t g = 0; g < graph_chunks; ++g) {
+        rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0x5eedULL + g, nullptr, d_ctr, s);
+        if (rc != GCQ_OK) { cudaStreamEndCapture(s, &graph); return fail(rc); }
+    }
+    if (cudaStreamEndCapture(s, &graph) != cudaSuccess) return fail(GCQ_ECUDA);
+    if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return fail(GCQ_ECUDA);
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return fail(GCQ_ECUDA);
+    using clk = std::chrono::steady_clock;
+    // warm-up
+    auto t0 = clk::now();
+    do {
+        if (cudaGraphLaunch(exec, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return fail(GCQ_ECUDA);
+    } while (std::chrono::duration<double, std::milli>(clk::now() - t0).count() < warmup_ms);
+    if (cudaMemsetAsync(d_ctr, 0, sizeof(gcq_tb_counters), s) != cudaSuccess) return fail(GCQ_ECUDA);
+    // timed window: graph replays until run_ms of host time
+    uint64_t reps = 0;
+    cudaEventRecord(e0, s);
+    t0 = clk::now();
+    do {
+        if (cudaGraphLaunch(exec, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return fail(GCQ_ECUDA);
+        ++reps;
+    } while (std::chrono::duration<double, std::milli>(clk::now() - t0).count() < run_ms);
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return fail(GCQ_ECUDA);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (cudaMemcpy(&out->counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(GCQ_ECUDA);
+    out->gpu_ms = ms;
+    out->launches = reps * graph_chunks;
+    uint32_t err = 0;
+    rc = read_error_word(q, s, &err);
+    cleanup();
+    if (rc != GCQ_OK) return rc;
+    return status_of(err);
+}
+
+int gcq_run_history(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops, int mode,
+                    int producer_percent, int value_mode, gcq_log_entry* host_out, size_t cap,
+                    size_t* n_out, void* stream) {
+    if (!q || !host_out || !n_out || threads == 0 || ops == 0 || block == 0 || block > 1024) return GCQ_EINVAL;
+    if (mode != 0 && mode != 1) return GCQ_EINVAL;
+    if (threads > q->max_threads) return GCQ_EINVAL;
+    if (q->kind == GCQ_SFQ && (threads > 32768u || ops > 0xFFFFu)) return GCQ_EUNSUPPORTED;  // history.cpp:285-292
+    const uint32_t stride = (mode == 0 ? 2u : 1u) * ops;
+    const size_t total = (size_t)threads * stride;
+    cudaStream_t s = gcqi::as_stream(stream);
+    int rc = gcq_reset(q, stream);
+    if (rc != GCQ_OK) return rc;
+    dbuf log, clk;
+    if (log.alloc(total * sizeof(gcq_log_entry)) != cudaSuccess || clk.alloc(256) != cudaSuccess) return GCQ_ENOMEM;
+    GCQ_CUDA(cudaMemsetAsync(log.p, 0, total * sizeof(gcq_log_entry), s));
+    const unsigned long long one = 1;
+    GCQ_CUDA(cudaMemcpyAsync(clk.p, &one, sizeof one, cudaMemcpyHostToDevice, s));
+    const unsigned grid = (threads + block - 1) / block;
+    rc = dispatch(q->kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_history<K><<<grid, block, 0, s>>>(q->obj, threads, ops, mode, producer_percent, value_mode,
+                                            (gcq_log_entry*)log.p, stride, (gcq::u64a*)clk.p);
+        return GCQ_OK;
+    });
+    GCQ_CUDA(cudaGetLastError());
+    std::vector<gcq_log_entry> h(total);
+    GCQ_CUDA(cudaMemcpyAsync(h.data(), log.p, total * sizeof(gcq_log_entry), cudaMemcpyDeviceToHost, s));
+    GCQ_CUDA(cudaStreamSynchronize(s));
+    uint32_t err = 0;
+    rc = read_error_word(q, s, &err);
+    if (rc != GCQ_OK) return rc;
+    // keep completed records and sort as wf_log_dump_jsonl does (history.cpp:257-267)
+    std::vector<gcq_log_entry> used;
+    used.reserve(total);
+    for (const auto& e : h) if (e.end != 0) used.push_back(e);
+    std::sort(used.begin(), used.end(), [](const gcq_log_entry& a, const gcq_log_entry& b) {
+        if (a.call != b.call) return a.call < b.call;
+        if (a.end != b.end) return a.end < b.end;
+        if (a.proc != b.proc) return a.proc < b.proc;
+        return a.op < b.op;
+    });
+    *n_out = used.size();
+    if (used.size() > cap) return GCQ_ECAPACITY;
+    memcpy(host_out, used.data(), used.size() * sizeof(gcq_log_entry));
+    return status_of(err);
+}
+
+int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
+                   gcq_fifo_result* out) {
+    if (!q || !out || threads == 0 || block == 0 || block > 1024) return GCQ_EINVAL;
+    if (threads > q->max_threads) return GCQ_EINVAL;
+    memset(out, 0, sizeof(*out));
+    // fifo_effective_ops_per_thread, throughout_bench.cpp:627-653
+    uint64_t ops = std::max<uint32_t>(1u, ops_per_thread);
+    if (q->kind != GCQ_WFQ) {
+        const uint64_t cap = 1ull << q->order;
+        const uint64_t lim = cap / threads;
+        if (lim == 0) { out->verified = -1; return GCQ_OK; }
+        ops = std::min<uint64_t>(ops, lim);
+    }
+    if (q->kind == GCQ_SFQ) {
+        if (threads > 32768u) { out->verified = -1; return GCQ_OK; }
+        ops = std::min<uint64_t>(ops, 0xFFFFu);
+    }
+    out->ops_per_thread = (uint32_t)ops;
+    const uint64_t total = (uint64_t)threads * ops;
+    out->in_count = total;
+    int rc = gcq_reset(q, nullptr);
+    if (rc != GCQ_OK) return rc;
+    dbuf counts, calls, ends, misc;
+    if (counts.alloc(total * 4) != cudaSuccess || calls.alloc(total * 8) != cudaSuccess ||
+        ends.alloc(total * 8) != cudaSuccess || misc.alloc(256) != cudaSuccess)
+        return GCQ_ENOMEM;
+    GCQ_CUDA(cudaMemset(counts.p, 0, total * 4));
+    GCQ_CUDA(cudaMemset(misc.p, 0, 256));
+    gcq::u64a* consumed = (gcq::u64a*)misc.p;
+    gcq::u64a* clock = consumed + 1;
+    gcq::u32a* oob = (gcq::u32a*)(consumed + 2);
+    const unsigned long long one = 1;
+    GCQ_CUDA(cudaMemcpy(clock, &one, 8, cudaMemcpyHostToDevice));
+    const unsigned grid = (threads + block - 1) / block;
+    const uint64_t tmo = std::max<uint64_t>(q->knobs.wait_timeout_ns, 1000000000ull) * 4;
+    rc = dispatch(q->kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_fifo_produce<K><<<grid, block>>>(q->obj, threads, (uint32_t)ops, tmo, q->err);
+        k_fifo_drain<K><<<grid, block>>>(q->obj, threads, (uint32_t)ops, total, (uint32_t*)counts.p,
+                                         (int64_t*)calls.p, (int64_t*)ends.p, consumed, clock, oob, tmo, q->err);
+        return GCQ_OK;
+    });
+    GCQ_CUDA(cudaGetLastError());
+    GCQ_CUDA(cudaDeviceSynchronize());
+    std::vector<uint32_t> hc(total);
+    std::vector<int64_t> hcall(total), hend(total);
+    uint64_t hmisc[4];
+    GCQ_CUDA(cudaMemcpy(hc.data(), counts.p, total * 4, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hcall.data(), calls.p, total * 8, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hend.data(), ends.p, total * 8, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hmisc, misc.p, sizeof hmisc, cudaMemcpyDeviceToHost));
+    out->out_count = std::min<uint64_t>(hmisc[0], total);
+    out->err_oob = (uint32_t)hmisc[2];
+    for (uint32_t p = 0; p < threads; ++p) {
+        int64_t max_call = -1;
+        for (uint64_t sq = 0; sq < ops; ++sq) {
+            const uint64_t slot = (uint64_t)p * ops + sq;
+            if (hc[slot] == 0) { out->err_missing++; continue; }
+            if (hc[slot] > 1) { out->err_gt1++; out->err_dup += hc[slot] - 1; }
+            if (hend[slot] < max_call) out->err_order++;
+            max_call = std::max(max_call, hcall[slot]);
+        }
+    }
+    uint32_t err = 0;
+    GCQ_CUDA(cudaMemcpy(&err, q->err, 4, cudaMemcpyDeviceToHost));
+    out->verified = (out->out_count == out->in_count && !out->err_oob && !out->err_dup && !out->err_order &&
+                     !out->err_missing && !out->err_gt1) ? 1 : 0;
+    return status_of(err);
+}
+
+}  // extern "C"

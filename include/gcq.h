@@ -1,0 +1,187 @@
+/* gcq.h: C ABI of libgcq.so, the GB300 (sm_103a) build of gCQ's GPU FIFO queues.
+ *
+ * The reference has no host API for its queues: each harness allocates a queue
+ * with hipMalloc, initialises it with a <<<1,1>>> kernel and calls the per-thread
+ * device API from its own kernels (throughout_bench.cpp:415-453, history.cpp:151-177,
+ * bfs_bench.cpp:723-737, rt_final.cpp:794-833).  This header is the boundary a host
+ * program (or a cgo/ctypes binding) uses instead: the library owns the device memory
+ * of a queue, callers hold an opaque handle, and the harness kernels of the four
+ * reference harnesses are exposed as calls.  Device code that wants the per-thread
+ * API links against include/gcq/*.cuh and gets the device-side queue from
+ * gcq_device_ptr().
+ *
+ * Conventions: every call returns GCQ_OK (0) or a negative gcq_status; no call
+ * exits the process (the reference's HIP_CHECK exits, throughout_bench.cpp:79-86).
+ * `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ * A handle may be used by one host thread at a time.
+ */
+#ifndef GCQ_H
+#define GCQ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Queue algorithms; names as in the reference Makefile's QUEUE knob (Makefile:67-81). */
+typedef enum { GCQ_GWFQ = 0, GCQ_GLFQ = 1, GCQ_WFQ = 2, GCQ_SFQ = 3 } gcq_kind;
+
+typedef enum {
+    GCQ_OK = 0,
+    GCQ_EINVAL = -1,        /* bad argument (capacity, thread count, mode) */
+    GCQ_ENOMEM = -2,        /* device or host allocation failed */
+    GCQ_ECUDA = -3,         /* a CUDA runtime call failed (see gcq_last_cuda_error) */
+    GCQ_ETIMEDOUT = -4,     /* a bounded device wait gave up (queue error word) */
+    GCQ_EDEVICE = -5,       /* the queue's device error word is set */
+    GCQ_EUNSUPPORTED = -6,  /* configuration outside the algorithm's envelope */
+    GCQ_ECAPACITY = -7      /* a harness input does not fit the queue */
+} gcq_status;
+
+/* Bits of the device error word (gcq_error_word). */
+#define GCQ_ERR_SPIN 0x1u      /* a retry loop hit its bound */
+#define GCQ_ERR_TIMEOUT 0x2u   /* a blocking wait passed its deadline */
+#define GCQ_ERR_TID 0x4u       /* a thread index >= max_threads */
+#define GCQ_ERR_POOL 0x8u      /* YMC cell pool exhausted (operations failed, as in the reference) */
+#define GCQ_ERR_CAPACITY 0x10u /* harness overflow (e.g. BFS frontier larger than the queue) */
+
+/* Compile-time knobs of the reference, here per queue at run time. */
+typedef struct gcq_knobs {
+    uint32_t help_delay;          /* G-WFQ WF_HELP_DELAY, gwf_queue.hpp:296-298 (64) */
+    uint32_t enq_patience;        /* G-WFQ WF_ENQ_PATIENCE, gwf_queue.hpp:300-302 (128) */
+    uint32_t deq_patience;        /* G-WFQ WF_DEQ_PATIENCE, gwf_queue.hpp:304-306 (256) */
+    uint32_t remap;               /* slot permutation: 0 identity (G-WFQ default, gwf_ring.hpp:43-50),
+                                     1 spread tickets over 128-B lines (G-LFQ default, glf_queue.hpp:116-120) */
+    uint32_t ymc_patience;        /* WF_PATIENCE, wfqueue_hip_opt.hpp:29-31 (16) */
+    uint32_t ymc_ops_per_thread;  /* WF_PREALLOC_OPS_PER_THREAD, wfqueue_hip_opt.hpp:33-35 (512) */
+    uint64_t wait_timeout_ns;     /* deadline of one blocking wait (SFQ), default 2 s */
+} gcq_knobs;
+
+typedef struct gcq_queue gcq_queue;
+
+/* Fill `k` with the reference defaults (remap follows the kind in gcq_create). */
+void gcq_default_knobs(gcq_knobs* k);
+
+/* Create a queue of 2^capacity_log2 elements usable by thread indices
+ * [0, max_threads).  Replaces the hipMalloc + queue_init_kernel<<<1,1>>> pair of
+ * throughout_bench.cpp:420-442 and the host initialisers wf_queue_host_init
+ * (wfqueue_hip_opt.hpp:594-644) and sfq_queue_host_init (sfqueue_hip.cpp:356-390).
+ * Envelope checks of the reference, made at run time:
+ *   G-WFQ: max_threads <= 2^capacity_log2 (gwf_queue.hpp:320) and the cycle-bit
+ *          inequality of gwf_queue.hpp:321-323;
+ *   SFQ:   MAX_ID >= 2 * (max_threads + 1) (sfqueue_hip.hpp:45-47).
+ * For YMC capacity_log2 is ignored; the pool holds
+ * max_threads * (3 * ymc_ops_per_thread + 128) cells plus 8 segments. */
+int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq_knobs* knobs,
+               gcq_queue** out);
+/* Free the queue's device memory (throughout_bench.cpp:444-453). */
+int gcq_destroy(gcq_queue* q);
+/* Re-initialise on `stream` with a grid-stride kernel (the reference re-runs its
+ * serial init, bfs_bench.cpp:531-552). */
+int gcq_reset(gcq_queue* q, void* stream);
+/* Device address of the queue object for kernels using include/gcq/*.cuh:
+ * gcq::gwf::mpmc*, gcq::glf::mpmc*, gcq::ymc::queue* or gcq::sfq::queue*. */
+int gcq_device_ptr(gcq_queue* q, void** dev);
+/* Read (and optionally clear) the device error word; synchronises the device. */
+int gcq_error_word(gcq_queue* q, uint32_t* err, int clear);
+/* Bytes of device memory held by the queue. */
+uint64_t gcq_device_bytes(const gcq_queue* q);
+/* Kind, capacity_log2 and max_threads the queue was created with. */
+int gcq_info(const gcq_queue* q, int* kind, uint32_t* capacity_log2, uint32_t* max_threads);
+const char* gcq_strerror(int status);
+/* Text of the last failing CUDA call in this process ("" if none). */
+const char* gcq_last_cuda_error(void);
+
+/* ---------------------------------------------------------------- history ----
+ * One record per completed operation, the fields of WFLogEntry
+ * (correctness/wf_linlog.hpp:7-14) and of the JSONL line
+ * (correctness/history.cpp:271-280): op 0 enqueue (ret 1 ok / 0 failed),
+ * op 1 dequeue (ret value or 0 for empty), op 2 dequeue that failed without
+ * effect (SFQ's BUSY; the reference writes it as op 1 ret 0). */
+typedef struct gcq_log_entry {
+    uint64_t proc;
+    uint32_t op;
+    uint32_t _pad;
+    uint64_t arg;
+    uint64_t ret;
+    int64_t call;   /* logical clock at call */
+    int64_t end;    /* logical clock at return */
+} gcq_log_entry;
+
+/* History kernel of correctness/history.cpp:188-227 on `threads` threads (block
+ * `block`), `ops` operations each: mode 0 alternating enqueue/dequeue, mode 1 the
+ * first producer_percent % of threads enqueue and the rest dequeue.  Values:
+ * value_mode 0 = (tid << 32) | (seq + 1) (history.cpp:184), 1 = 32-bit
+ * (tid << 16) | (seq + 1); SFQ always uses the 15+16-bit encoding of
+ * history.cpp:121-140 and its non-blocking operations.  Every event is bracketed
+ * by a device-wide logical clock (wf_linlog.hpp:25-45).  Records with end != 0
+ * are sorted by (call, end, proc, op) as history.cpp:257-267 does and copied to
+ * host_out (capacity `cap`); *n_out receives the count.  The queue is reset first. */
+int gcq_run_history(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops, int mode,
+                    int producer_percent, int value_mode, gcq_log_entry* host_out, size_t cap,
+                    size_t* n_out, void* stream);
+
+/* ------------------------------------------------------------- throughput ----
+ * Counters of throughout_bench.cpp:775-785. */
+typedef struct gcq_tb_counters {
+    uint64_t enq_success, enq_fail, deq_success, deq_empty;
+} gcq_tb_counters;
+
+/* One chunk launch of balanced_chunk_kernel (mode 0, throughout_bench.cpp:810-840)
+ * or split_chunk_kernel (mode 1, :842-882): each of `threads` threads does
+ * chunk_ops iterations; payloads are uint32 splitmix64(seed, tid, i) values.
+ * Counters accumulate into dev_counters (device memory, gcq_tb_counters layout).
+ * SFQ uses blocking operations in mode 0 and non-blocking ones in mode 1, as the
+ * reference does; blocking SFQ needs every thread resident, so mode 0 with more
+ * threads than the device can hold at once returns GCQ_EUNSUPPORTED. */
+int gcq_tb_launch(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                  uint32_t chunk_ops, uint64_t seed, void* dev_counters, void* stream);
+
+/* End-to-end chunk through host memory: copies threads*chunk_ops uint32 payloads
+ * (payload i of thread t at host_payloads[i * threads + t]) to the device, runs
+ * one chunk with them, and copies the counters of that chunk back to host_counters.
+ * host_payloads should be pinned for full copy bandwidth. */
+int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                      uint32_t chunk_ops, const uint32_t* host_payloads, gcq_tb_counters* host_counters,
+                      void* stream);
+
+typedef struct gcq_tb_result {
+    gcq_tb_counters counters;
+    double gpu_ms;       /* CUDA-event time of the timed window */
+    uint64_t launches;   /* chunk launches in the timed window */
+} gcq_tb_result;
+
+/* Fixed-duration run of run_balanced_timed / run_split_timed
+ * (throughout_bench.cpp:959-1051): warm up for warmup_ms, zero the counters, then
+ * replay a CUDA graph of `graph_chunks` chunk launches until run_ms of host time
+ * has passed.  The reference launches and synchronises every chunk from the host. */
+int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+               uint32_t chunk_ops, double warmup_ms, double run_ms, uint32_t graph_chunks,
+               gcq_tb_result* out);
+
+/* ------------------------------------------------------------- FIFO check ----
+ * Produce-then-drain check of throughout_bench.cpp:456-767 (MODE_FIFO).  Every
+ * thread enqueues ops_per_thread tokens (tid << 32 | seq + 1; SFQ 15+16 bits),
+ * then all threads drain.  Exactly-once as in the reference (in/out counts,
+ * duplicates, missing, out-of-range).  err_order counts token pairs of one
+ * producer, seq a < seq b, where the dequeue of b returned before the dequeue of a
+ * was called (logical clock); the reference's atomicMax order check (:585-588)
+ * starts from 0xFFFFFFFF (:691) and never fires.  ops_per_thread is capped to
+ * capacity / threads for bounded queues (:627-653); 0 after the cap = skipped. */
+typedef struct gcq_fifo_result {
+    uint64_t in_count, out_count;
+    uint32_t err_oob, err_dup, err_order, err_missing, err_gt1;
+    uint32_t ops_per_thread;   /* after the capacity cap */
+    int verified;              /* 1 = YES, 0 = NO, -1 = skipped */
+    int _pad;
+} gcq_fifo_result;
+
+int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
+                   gcq_fifo_result* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCQ_H */

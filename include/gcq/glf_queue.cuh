@@ -1,0 +1,213 @@
+// G-LFQ for sm_103a: the lock-free SCQ queue of glf_queue.hpp with
+// warp-aggregated tickets, 64-bit entries {Cycle8, Safe1, Index32}, no slow path.
+//
+// Kept from the reference: entry layout and INIT (glf_queue.hpp:66-90), modular
+// cycles (:96-110), the line-spreading slot permutation (:116-120), ring and
+// indirection layout (:126-138), enqueue/dequeue loops (:467-560), 64-bit payload
+// indirection (:566-582).
+// Changed for GB300: ring capacity and the permutation are runtime header fields;
+// the permutation spreads over 128-byte lines (16 entries) by default; Tail, Head
+// and Threshold own separate lines; loads are acquire/relaxed loads instead of
+// atomicAdd(p, 0) (:144-148); retry loops are bounded (GCQ_SPIN_LIMIT) and report
+// through the header's error word instead of spinning forever.
+#pragma once
+
+#include <stdint.h>
+#include "gcq_atomics.cuh"
+
+#ifndef FQ_N
+#define FQ_N 32768
+#endif
+#ifndef FQ_CYCLE_BITS
+#define FQ_CYCLE_BITS 8
+#endif
+
+namespace gcq {
+namespace glf {
+
+constexpr uint32_t CYCLE_MASK = (1u << FQ_CYCLE_BITS) - 1;
+constexpr uint32_t HALF_CYCLE = 1u << (FQ_CYCLE_BITS - 1);
+constexpr uint32_t BOT = 0xFFFFFFFEu;
+constexpr uint32_t BOT_C = 0xFFFFFFFFu;
+
+namespace ent {
+constexpr int CYCLE_SHIFT = 48, SAFE_SHIFT = 47;
+constexpr uint64_t SAFE_BIT = 1ULL << SAFE_SHIFT;
+constexpr uint64_t CONSUME_MASK = (uint64_t)BOT_C;
+constexpr uint64_t INIT = SAFE_BIT | (uint64_t)BOT;
+__host__ __device__ __forceinline__ uint32_t cycle(uint64_t e) { return (uint32_t)(e >> CYCLE_SHIFT) & CYCLE_MASK; }
+__host__ __device__ __forceinline__ bool safe(uint64_t e) { return (e >> SAFE_SHIFT) & 1; }
+__host__ __device__ __forceinline__ uint32_t index(uint64_t e) { return (uint32_t)e; }
+__host__ __device__ __forceinline__ uint64_t pack(uint32_t c, bool s, uint32_t i) {
+    return ((uint64_t)(c & CYCLE_MASK) << CYCLE_SHIFT) | ((uint64_t)s << SAFE_SHIFT) | (uint64_t)i;
+}
+}  // namespace ent
+
+__host__ __device__ __forceinline__ int cycle_cmp(uint32_t a, uint32_t b) {
+    const uint32_t d = (a - b) & CYCLE_MASK;
+    return d == 0 ? 0 : (d < HALF_CYCLE ? 1 : -1);
+}
+
+struct alignas(128) ring {
+    u64a Tail;
+    char _pad0[120];
+    u64a Head;
+    char _pad1[120];
+    int Threshold;
+    char _pad2[124];
+    u64a* Entry;          // 2N slots
+    u32a* err;
+    uint32_t order;       // log2 N
+    uint32_t line_log2;   // log2 entries per line for the permutation; 0 = identity
+    char _pad3[104];
+};
+
+struct alignas(128) mpmc {
+    ring aq;
+    ring fq;
+    u64a* data;
+    u32a* err;
+};
+
+struct cfg {
+    u64a* entry;
+    u32a* err;
+    uint32_t order, line_log2;
+    __host__ __device__ __forceinline__ uint32_t slots() const { return 2u << order; }
+    __host__ __device__ __forceinline__ int32_t threshold_max() const { return 3 * (int32_t)(1u << order) - 1; }
+    __host__ __device__ __forceinline__ uint32_t cycle_of(uint64_t t) const { return (uint32_t)(t >> (order + 1)) & CYCLE_MASK; }
+    // cache_remap, glf_queue.hpp:116-120
+    __host__ __device__ __forceinline__ uint32_t slot_of(uint64_t t) const {
+        const uint32_t pos = (uint32_t)t & (slots() - 1);
+        if (line_log2 == 0 || slots() <= (1u << line_log2)) return pos;
+        const uint32_t per = 1u << line_log2;
+        return (pos & (per - 1)) * (slots() >> line_log2) + (pos >> line_log2);
+    }
+    __host__ __device__ __forceinline__ uint32_t pos_of_slot(uint32_t s) const {
+        if (line_log2 == 0 || slots() <= (1u << line_log2)) return s;
+        const uint32_t stride = slots() >> line_log2;
+        return (s % stride) * (1u << line_log2) + s / stride;
+    }
+};
+
+__device__ __forceinline__ cfg load_cfg(const ring* q) {
+    cfg c;
+    c.entry = q->Entry; c.err = q->err; c.order = q->order; c.line_log2 = q->line_log2;
+    return c;
+}
+
+// fq_ring_init_empty / fq_ring_init_full (glf_queue.hpp:418-435), split over a
+// grid-stride group; each slot's final value is computed directly.
+__device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nthreads) {
+    const cfg c = load_cfg(q);
+    const uint32_t slots = c.slots(), n = 1u << c.order;
+    for (uint64_t s = gid; s < slots; s += nthreads) {
+        const uint32_t pos = c.pos_of_slot((uint32_t)s);
+        c.entry[s] = (full && pos < n) ? ent::pack(c.cycle_of((uint64_t)slots + pos), true, pos) : ent::INIT;
+    }
+    if (gid == 0) {
+        q->Head = slots;
+        q->Tail = full ? (uint64_t)slots + n : (uint64_t)slots;
+        q->Threshold = full ? c.threshold_max() : -1;
+    }
+}
+
+// catchup, glf_queue.hpp:447-455
+__device__ inline void catchup(ring* q, uint64_t tail, uint64_t head) {
+    for (int i = 0; i < 32; i++) {
+        if (cas_ok(&q->Tail, tail, head)) break;
+        head = ld_acq(&q->Head);
+        tail = ld_acq(&q->Tail);
+        if (tail >= head) break;
+    }
+}
+
+// fq_enqueue, glf_queue.hpp:467-500.  Returns false only if the retry bound was
+// reached (error word set).
+__device__ inline bool enqueue(ring* q, uint32_t index) {
+    const cfg c = load_cfg(q);
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        const uint64_t T = warp_fetch_add(&q->Tail, 1);
+        const uint32_t tcyc = c.cycle_of(T);
+        const uint32_t j = c.slot_of(T);
+        uint64_t E = ld_rlx(&c.entry[j]);
+        for (;; ++spin) {
+            const uint32_t ecyc = ent::cycle(E), eidx = ent::index(E);
+            if (cycle_cmp(ecyc, tcyc) >= 0 || eidx < BOT) break;
+            if (!ent::safe(E)) {
+                dekker_fence();
+                if (ld_acq(&q->Head) > T) break;
+            }
+            if (!cas_upd(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
+                if (spin >= GCQ_SPIN_LIMIT) break;
+                continue;
+            }
+            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            return true;
+        }
+    }
+    raise_error(c.err, ERR_SPIN);
+    return false;
+}
+
+// fq_dequeue, glf_queue.hpp:510-560.  Returns the index or BOT when empty.
+__device__ inline uint32_t dequeue(ring* q) {
+    if (ld_acq(&q->Threshold) < 0) return BOT;
+    const cfg c = load_cfg(q);
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        const uint64_t H = warp_fetch_add(&q->Head, 1);
+        const uint32_t hcyc = c.cycle_of(H);
+        const uint32_t j = c.slot_of(H);
+        uint64_t E = ld_acq(&c.entry[j]);
+        for (;; ++spin) {
+            const uint32_t ecyc = ent::cycle(E), eidx = ent::index(E);
+            if (cycle_cmp(ecyc, hcyc) == 0 && eidx < BOT) {
+                fetch_or(&c.entry[j], ent::CONSUME_MASK);
+                return eidx;
+            }
+            if (cycle_cmp(ecyc, hcyc) >= 0 || spin >= GCQ_SPIN_LIMIT) break;
+            const uint64_t nw = (eidx >= BOT) ? ent::pack(hcyc, ent::safe(E), BOT) : ent::pack(ecyc, false, eidx);
+            if (cas_upd(&c.entry[j], &E, nw)) break;
+        }
+        dekker_fence();
+        const uint64_t T = ld_acq(&q->Tail);
+        if (T <= H + 1) {
+            catchup(q, T, H + 1);
+            fetch_add(&q->Threshold, -1);
+            return BOT;
+        }
+        if (fetch_add(&q->Threshold, -1) <= 0) return BOT;
+    }
+    raise_error(c.err, ERR_SPIN);
+    return BOT;
+}
+
+// fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582
+__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) {
+    const uint32_t idx = dequeue(&q->fq);
+    if (idx == BOT) return false;
+    st_rlx(&q->data[idx], value);
+    return enqueue(&q->aq, idx);
+}
+__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out) {
+    const uint32_t idx = dequeue(&q->aq);
+    if (idx == BOT) return false;
+    *out = ld_rlx(&q->data[idx]);
+    enqueue(&q->fq, idx);
+    return true;
+}
+
+}  // namespace glf
+}  // namespace gcq
+
+// -----------------------------------------------------------------------------
+// Reference-named device API (glf_queue.hpp:418-582) over the runtime rings.
+// -----------------------------------------------------------------------------
+typedef gcq::glf::ring fq_ring_t;
+typedef gcq::glf::mpmc fq_mpmc_t;
+static constexpr uint32_t FQ_BOT = gcq::glf::BOT;
+static constexpr uint32_t FQ_BOT_C = gcq::glf::BOT_C;
+__device__ __forceinline__ void fq_enqueue(fq_ring_t* q, uint32_t index) { gcq::glf::enqueue(q, index); }
+__device__ __forceinline__ uint32_t fq_dequeue(fq_ring_t* q) { return gcq::glf::dequeue(q); }
+__device__ __forceinline__ bool fq_enqueue_ptr(fq_mpmc_t* q, uint64_t v) { return gcq::glf::enqueue_ptr(q, v); }
+__device__ __forceinline__ bool fq_dequeue_ptr(fq_mpmc_t* q, uint64_t* out) { return gcq::glf::dequeue_ptr(q, out); }

@@ -1,0 +1,497 @@
+// G-WFQ algorithm for sm_103a: fast path (SCQ with warp-aggregated tickets),
+// cooperative slow path (wCQ's two-phase fetch-and-add), helping, and the 64-bit
+// payload indirection.  Every function names the reference routine it restates.
+//
+// Thread identity: the per-thread calls take the caller's thread index `tid`
+// explicitly (it selects the help record; it must be below the ring's
+// max_threads).  The reference-named wrappers at the end use wf_tid(), the global
+// x index, or WF_TID_EXPR when defined (gwf_ring.hpp:53-63).
+#pragma once
+
+#include "gwf_queue.cuh"
+
+namespace gcq {
+namespace gwf {
+
+using entry::BOT;
+using entry::BOT_C;
+
+// ------------------------------------------------------------------ init
+// Thread `gid` of a `nthreads`-wide grid-stride group initialises its share of the
+// ring; the reference does the same serially on one thread (gwf_ring.hpp:229-276).
+// With `full` the ring starts holding indices 0..N-1 at tickets 2N..3N-1, as
+// wf_mpmc_init does for fq (gwf_ring.hpp:278-298).  Each slot's final value is
+// computed from the slot itself (inverse of slot_of), so no two threads write the
+// same word and no grid-wide ordering is needed.
+__device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nthreads) {
+    const cfg c = load_cfg(q);
+    const uint32_t slots = c.slots();
+    const uint32_t n = 1u << c.order;
+    for (uint64_t s = gid; s < slots; s += nthreads) {
+        const uint32_t pos = c.pos_of_slot((uint32_t)s);
+        c.entry[s] = (full && pos < n)
+                         ? entry::pack(0xFF, c.cycle_of((uint64_t)slots + pos), true, true, pos)
+                         : entry::INIT;
+    }
+    for (uint64_t i = gid; i < c.max_threads; i += nthreads) {
+        record* r = &c.rec[i];
+        r->seq1 = 1; r->enqueue = 0; r->pending = 0; r->index = 0;
+        r->localTail = 0; r->initTail = 0; r->localHead = 0; r->initHead = 0;
+        r->seq2 = 0;
+        r->p2_seq1 = 1; r->p2_local = 0; r->p2_cnt = 0; r->p2_seq2 = 0;
+        c.help[i].nextCheck = (int32_t)c.help_delay;
+        c.help[i].nextTid = (uint32_t)i;
+    }
+    if (gid == 0) {
+        const uint64_t start = slots;
+        q->Head = c.pack_global(start, c.null_tid());
+        q->Tail = c.pack_global(full ? start + n : start, c.null_tid());
+        q->Threshold = full ? c.threshold_max() : -1;
+    }
+}
+
+// ------------------------------------------------------------------ consume etc.
+// finalize_request, gwf_ring.hpp:309-328: set FIN on the slow-path enqueuer whose
+// localTail holds ticket h.
+__device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t tid) {
+    const uint64_t h_local = h_raw << 2;
+    uint32_t i = (tid + 1 == c.max_threads) ? 0 : tid + 1;
+    while (i != tid) {
+        const uint64_t lt = ld_acq(&c.rec[i].localTail);
+        if ((lt & local::CNT_MASK) == h_local) {
+            cas(&c.rec[i].localTail, h_local, h_local | local::FIN);
+            return;
+        }
+        i = (i + 1 == c.max_threads) ? 0 : i + 1;
+    }
+}
+
+// consume, gwf_ring.hpp:335-341
+__device__ __forceinline__ void consume(const cfg& c, uint64_t h_raw, uint32_t j, uint64_t e, uint32_t tid) {
+    if (!entry::enq(e)) finalize_request(c, h_raw, tid);
+    fetch_or(&c.entry[j], entry::CONSUME_MASK);
+}
+
+// catchup, gwf_ring.hpp:348-371
+__device__ inline void catchup(ring* q, const cfg& c, uint64_t tail_raw, uint64_t head_raw) {
+    for (int i = 0; i < 32; i++) {
+        uint64_t cur = ld_acq(&q->Tail);
+        const uint64_t cur_cnt = c.counter(cur);
+        if (cur_cnt >= head_raw) break;
+        if (cur_cnt != tail_raw) {
+            tail_raw = cur_cnt;
+            head_raw = c.counter(ld_acq(&q->Head));
+            if (tail_raw >= head_raw) break;
+            continue;
+        }
+        if (cas_ok(&q->Tail, cur, c.pack_global(head_raw, c.thridx(cur)))) break;
+        head_raw = c.counter(ld_acq(&q->Head));
+        tail_raw = c.counter(ld_acq(&q->Tail));
+        if (tail_raw >= head_raw) break;
+    }
+}
+
+// ------------------------------------------------------------------ fast path
+// try_enq, gwf_ring.hpp:382-414.  0 on success, else the ticket tried.
+__device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
+    const uint64_t T = c.counter(warp_fetch_add(&q->Tail, c.cinc()));
+    const uint32_t tcyc = c.cycle_of(T);
+    const uint32_t j = c.slot_of(T);
+    uint64_t E = ld_rlx(&c.entry[j]);
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        const uint32_t ecyc = entry::cycle(E);
+        const uint32_t eidx = entry::index(E);
+        if (cycle_cmp(ecyc, tcyc) >= 0 || !entry::empty_index(eidx)) return T;
+        if (!entry::safe(E)) {
+            dekker_fence();
+            if (c.counter(ld_acq(&q->Head)) > T) return T;
+        }
+        const uint64_t nw = entry::pack(entry::note(E), tcyc, true, true, index);
+        if (!cas_upd(&c.entry[j], &E, nw)) continue;
+        if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+        return 0;
+    }
+    raise_error(c.err, ERR_SPIN);
+    return T;
+}
+
+// try_deq, gwf_ring.hpp:421-472.  0 when finished (*out = index, or BOT if the
+// queue is empty), else the ticket tried.
+__device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_t tid) {
+    const uint64_t H = c.counter(warp_fetch_add(&q->Head, c.cinc()));
+    const uint32_t hcyc = c.cycle_of(H);
+    const uint32_t j = c.slot_of(H);
+    uint64_t E = ld_acq(&c.entry[j]);
+    uint32_t spin = 0;
+    for (;; ++spin) {
+        const uint32_t ecyc = entry::cycle(E);
+        const uint32_t eidx = entry::index(E);
+        if (cycle_cmp(ecyc, hcyc) == 0 && !entry::empty_index(eidx)) {
+            consume(c, H, j, E, tid);
+            *out = eidx;
+            return 0;
+        }
+        if (cycle_cmp(ecyc, hcyc) >= 0) break;
+        if (spin >= GCQ_SPIN_LIMIT) { raise_error(c.err, ERR_SPIN); break; }
+        const uint64_t nw = entry::empty_index(eidx)
+                                ? entry::pack(entry::note(E), hcyc, entry::safe(E), true, BOT)
+                                : entry::pack(entry::note(E), ecyc, false, entry::enq(E), eidx);
+        if (cas_upd(&c.entry[j], &E, nw)) break;
+    }
+    dekker_fence();
+    const uint64_t T = c.counter(ld_acq(&q->Tail));
+    if (T <= H + 1) {
+        catchup(q, c, T, H + 1);
+        fetch_add(&q->Threshold, -1);
+        *out = BOT;
+        return 0;
+    }
+    if (fetch_add(&q->Threshold, -1) <= 0) {
+        *out = BOT;
+        return 0;
+    }
+    return H;
+}
+
+// ------------------------------------------------------------------ slow path
+// prepare_phase2, gwf_ring.hpp:486-504: publish (local, cnt) under a sequence pair.
+__device__ __forceinline__ void prepare_phase2(record* me, u64a* localp, uint64_t cnt_local) {
+    const uint32_t seq = ld_rlx(&me->p2_seq1) + 1;
+    st_rlx(&me->p2_seq1, seq);
+    fence_acq_rel();
+    st_rlx(&me->p2_local, (uint64_t)(uintptr_t)localp);
+    st_rlx(&me->p2_cnt, cnt_local);
+    st_rel(&me->p2_seq2, seq);
+}
+
+// slow_faa, gwf_ring.hpp:523-639: cooperative fetch-and-add on Tail/Head that
+// increments the global counter exactly once per helper group.  Returns false
+// when the request was finalised (FIN), true when *v holds a fresh ticket.
+__device__ inline bool slow_faa(ring* q, const cfg& c, u64a* globalp, u64a* localp, uint64_t* v,
+                                int* thld, uint32_t tid) {
+    record* my = &c.rec[tid];
+    uint64_t cnt_local = 0, cnt_raw = 0;
+    bool global_ok = false;
+    uint32_t spin = 0;
+    do {
+        if (++spin > GCQ_SPIN_LIMIT) {
+            raise_error(c.err, ERR_SPIN);
+            *v = ld_acq(localp) | local::FIN;
+            return false;
+        }
+        const uint64_t lc = ld_acq(localp);
+        if (lc & local::FIN) { *v = lc; return false; }
+        uint64_t gp = ld_acq(globalp);
+        const uint32_t gt = c.thridx(gp);
+        if (gt != (uint32_t)c.null_tid()) {
+            // help the phase-2 request named by the global word (gwf_ring.hpp:550-590)
+            record* hr = &c.rec[gt];
+            const uint32_t seq = ld_acq(&hr->p2_seq2);
+            u64a* p2_local = (u64a*)(uintptr_t)ld_rlx(&hr->p2_local);
+            const uint64_t p2_cnt = ld_rlx(&hr->p2_cnt);
+            fence_acq_rel();
+            const uint32_t seq1 = ld_rlx(&hr->p2_seq1);
+            if (seq1 == seq && p2_local) cas(p2_local, p2_cnt | local::INC, p2_cnt);
+            const uint64_t clean = c.pack_global(c.counter(gp), c.null_tid());
+            if (!cas_ok(globalp, gp, clean)) continue;
+            gp = clean;
+        }
+        cnt_raw = c.counter(gp);
+        cnt_local = cnt_raw << 2;
+        uint64_t vc = *v;
+        if (!cas_upd(localp, &vc, cnt_local | local::INC)) {
+            *v = vc;
+            if (vc & local::FIN) return false;
+            if (!(vc & local::INC)) return true;
+            cnt_local = vc & local::CNT_MASK;
+            cnt_raw = cnt_local >> 2;
+        } else {
+            *v = cnt_local | local::INC;
+        }
+        prepare_phase2(my, localp, cnt_local);
+        global_ok = cas_ok(globalp, c.pack_global(cnt_raw, c.null_tid()), c.pack_global(cnt_raw + 1, tid));
+    } while (!global_ok);
+    if (thld) fetch_add(thld, -1);
+    cas(localp, cnt_local | local::INC, cnt_local);
+    cas(globalp, c.pack_global(cnt_raw + 1, tid), c.pack_global(cnt_raw + 1, c.null_tid()));
+    *v = cnt_local;
+    return true;
+}
+
+// try_enq_slow, gwf_ring.hpp:650-705
+__device__ inline bool try_enq_slow(ring* q, const cfg& c, uint64_t T_raw, uint32_t index, record* r) {
+    const uint32_t tcyc = c.cycle_of(T_raw);
+    const uint32_t j = c.slot_of(T_raw);
+    uint64_t P = ld_acq(&c.entry[j]);
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        const uint32_t ecyc = entry::cycle(P), enote = entry::note(P), eidx = entry::index(P);
+        if (cycle_cmp(ecyc, tcyc) < 0 && cycle_cmp(enote, tcyc) < 0) {
+            bool skip = !entry::empty_index(eidx);
+            if (!skip && !entry::safe(P)) {
+                dekker_fence();
+                skip = c.counter(ld_acq(&q->Head)) > T_raw;
+            }
+            if (skip) {
+                // advance Note so later helpers skip this slot too
+                const uint64_t nn = entry::pack(tcyc, ecyc, entry::safe(P), entry::enq(P), eidx);
+                if (!cas_upd(&c.entry[j], &P, nn)) continue;
+                return false;
+            }
+            // two-step insertion: Enq=0 first, flipped to 1 once FIN is set
+            const uint64_t nn = entry::pack(enote, tcyc, true, false, index);
+            if (!cas_upd(&c.entry[j], &P, nn)) continue;
+            const uint64_t T_local = T_raw << 2;
+            if (cas_ok(&r->localTail, T_local, T_local | local::FIN))
+                cas(&c.entry[j], nn, entry::pack(enote, tcyc, true, true, index));
+            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            return true;
+        }
+        return cycle_cmp(ecyc, tcyc) == 0;
+    }
+    raise_error(c.err, ERR_SPIN);
+    return true;
+}
+
+// try_deq_slow, gwf_ring.hpp:712-769
+__device__ inline bool try_deq_slow(ring* q, const cfg& c, uint64_t H_raw, record* r) {
+    const uint32_t hcyc = c.cycle_of(H_raw);
+    const uint32_t j = c.slot_of(H_raw);
+    uint64_t P = ld_acq(&c.entry[j]);
+    for (uint32_t spin = 0;; ++spin) {
+        if (spin >= GCQ_SPIN_LIMIT) { raise_error(c.err, ERR_SPIN); break; }
+        const uint32_t ecyc = entry::cycle(P), enote = entry::note(P), eidx = entry::index(P);
+        if (cycle_cmp(ecyc, hcyc) == 0 && !entry::empty_index(eidx)) {
+            const uint64_t H_local = H_raw << 2;
+            cas(&r->localHead, H_local, H_local | local::FIN);
+            return true;
+        }
+        uint32_t n_note = enote;
+        uint64_t val = entry::pack(n_note, hcyc, entry::safe(P), true, BOT);
+        if (!entry::empty_index(eidx)) {
+            if (cycle_cmp(ecyc, hcyc) < 0 && cycle_cmp(enote, hcyc) < 0) {
+                const uint64_t nn = entry::pack(hcyc, ecyc, entry::safe(P), entry::enq(P), eidx);
+                if (!cas_upd(&c.entry[j], &P, nn)) continue;
+                n_note = hcyc;
+            }
+            val = entry::pack(n_note, ecyc, false, entry::enq(P), eidx);
+        }
+        if (cycle_cmp(ecyc, hcyc) < 0) {
+            if (!cas_upd(&c.entry[j], &P, val)) continue;
+        }
+        break;
+    }
+    dekker_fence();
+    const uint64_t T = c.counter(ld_acq(&q->Tail));
+    if (T <= H_raw + 1) catchup(q, c, T, H_raw + 1);
+    if (ld_acq(&q->Threshold) < 0) {
+        const uint64_t H_local = H_raw << 2;
+        cas(&r->localHead, H_local, H_local | local::FIN);
+        return true;
+    }
+    return false;
+}
+
+// enqueue_slow / dequeue_slow, gwf_ring.hpp:775-802
+__device__ inline void enqueue_slow(ring* q, const cfg& c, uint64_t v, uint32_t index, record* r, uint32_t tid) {
+    while (slow_faa(q, c, &q->Tail, &r->localTail, &v, nullptr, tid))
+        if (try_enq_slow(q, c, v >> 2, index, r)) break;
+}
+__device__ inline void dequeue_slow(ring* q, const cfg& c, uint64_t v, record* r, uint32_t tid) {
+    while (slow_faa(q, c, &q->Head, &r->localHead, &v, &q->Threshold, tid))
+        if (try_deq_slow(q, c, v >> 2, r)) break;
+}
+
+// ------------------------------------------------------------------ helping
+// help_enqueue / help_dequeue / help_threads, gwf_ring.hpp:808-861
+__device__ inline void help_enqueue(ring* q, const cfg& c, record* thr, uint32_t tid) {
+    const uint32_t seq = ld_acq(&thr->seq2);
+    const uint32_t is_enq = ld_rlx(&thr->enqueue);
+    const uint32_t idx = ld_rlx(&thr->index);
+    const uint64_t init_tail = ld_rlx(&thr->initTail);
+    fence_acq_rel();
+    if (is_enq && ld_rlx(&thr->seq1) == seq) enqueue_slow(q, c, init_tail, idx, thr, tid);
+}
+__device__ inline void help_dequeue(ring* q, const cfg& c, record* thr, uint32_t tid) {
+    const uint32_t seq = ld_acq(&thr->seq2);
+    const uint32_t is_enq = ld_rlx(&thr->enqueue);
+    const uint64_t init_head = ld_rlx(&thr->initHead);
+    fence_acq_rel();
+    if (!is_enq && ld_rlx(&thr->seq1) == seq) dequeue_slow(q, c, init_head, thr, tid);
+}
+__device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid) {
+    helper_state hs = c.help[tid];
+    if (--hs.nextCheck != 0) {
+        c.help[tid].nextCheck = hs.nextCheck;
+        return;
+    }
+    record* thr = &c.rec[hs.nextTid];
+    if (ld_acq(&thr->pending)) {
+        if (ld_rlx(&thr->enqueue)) help_enqueue(q, c, thr, tid);
+        else help_dequeue(q, c, thr, tid);
+    }
+    hs.nextCheck = (int32_t)c.help_delay;
+    hs.nextTid = (hs.nextTid + 1 == c.max_threads) ? 0 : hs.nextTid + 1;
+    c.help[tid] = hs;
+}
+
+// ------------------------------------------------------------------ top level
+// Enqueue_wf, gwf_ring.hpp:1234-1284
+__device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
+    const cfg c = load_cfg(q);
+    if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return; }
+    help_threads(q, c, tid);
+    uint64_t tail = 0;
+    for (uint32_t count = c.enq_patience; --count != 0;) {
+        tail = try_enq(q, c, index);
+        if (tail == 0) return;
+    }
+    record* r = &c.rec[tid];
+    const uint32_t seq = ld_rlx(&r->seq1);
+    const uint64_t tail_local = tail << 2;
+    st_rlx(&r->localTail, tail_local);
+    st_rlx(&r->initTail, tail_local);
+    st_rlx(&r->index, index);
+    st_rlx(&r->enqueue, 1u);
+    st_rel(&r->seq2, seq);
+    st_rel(&r->pending, 1u);
+    enqueue_slow(q, c, tail_local, index, r, tid);
+    st_rel(&r->pending, 0u);
+    st_rel(&r->seq1, seq + 1);
+}
+
+// Dequeue_wf, gwf_ring.hpp:1286-1356.  Returns the index or BOT when empty.
+__device__ inline uint32_t dequeue(ring* q, uint32_t tid) {
+    const cfg c = load_cfg(q);
+    if (ld_acq(&q->Threshold) < 0) return BOT;
+    if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return BOT; }
+    help_threads(q, c, tid);
+    uint32_t out = BOT;
+    uint64_t head = 0;
+    for (uint32_t count = c.deq_patience; --count != 0;) {
+        head = try_deq(q, c, &out, tid);
+        if (head == 0) return out;
+    }
+    record* r = &c.rec[tid];
+    const uint32_t seq = ld_rlx(&r->seq1);
+    const uint64_t head_local = head << 2;
+    st_rlx(&r->localHead, head_local);
+    st_rlx(&r->initHead, head_local);
+    st_rlx(&r->enqueue, 0u);
+    st_rel(&r->seq2, seq);
+    st_rel(&r->pending, 1u);
+    dequeue_slow(q, c, head_local, r, tid);
+    st_rel(&r->pending, 0u);
+    st_rel(&r->seq1, seq + 1);
+    // gather the slow-path result (gwf_ring.hpp:1340-1355)
+    const uint64_t h_raw = ld_acq(&r->localHead) >> 2;
+    const uint32_t j = c.slot_of(h_raw);
+    const uint64_t e = ld_acq(&c.entry[j]);
+    if (cycle_cmp(entry::cycle(e), c.cycle_of(h_raw)) == 0 && !entry::empty_index(entry::index(e))) {
+        consume(c, h_raw, j, e, tid);
+        return entry::index(e);
+    }
+    return BOT;
+}
+
+// Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.
+__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
+    const uint32_t idx = dequeue(&q->fq, tid);
+    if (idx == BOT) return false;
+    st_rlx(&q->data[idx], value);
+    enqueue(&q->aq, idx, tid);   // its acq_rel CAS publishes data[idx]
+    return true;
+}
+__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid) {
+    const uint32_t idx = dequeue(&q->aq, tid);
+    if (idx == BOT) return false;
+    *out = ld_rlx(&q->data[idx]);
+    enqueue(&q->fq, idx, tid);   // releases the slot only after the read above
+    return true;
+}
+
+}  // namespace gwf
+}  // namespace gcq
+
+// -----------------------------------------------------------------------------
+// Reference-named device API (gwf_queue.hpp:351-438).
+// -----------------------------------------------------------------------------
+#ifdef WF_TID_EXPR
+__device__ __forceinline__ uint32_t wf_tid() { return (uint32_t)(WF_TID_EXPR); }
+#else
+__device__ __forceinline__ uint32_t wf_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+#endif
+
+// Serial single-thread initialisation, as the reference's <<<1,1>>> init kernels do.
+template <typename Config, uint32_t N_PARAM>
+__device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
+    gcq::gwf::ring* h = &q->hdr;
+    h->Entry = q->Entry;
+    h->Record = q->Record;
+    h->Help = q->Help;
+    q->err = 0;
+    h->err = &q->err;
+    h->order = 31 - __clz(N_PARAM);
+    h->thr_bits = Config::BITS;
+    h->max_threads = Config::MAX_THREADS;
+    h->help_delay = WF_HELP_DELAY;
+    h->enq_patience = WF_ENQ_PATIENCE;
+    h->deq_patience = WF_DEQ_PATIENCE;
+#ifdef CACHE_REMAP
+    h->remap = 1;
+#else
+    h->remap = 0;
+#endif
+    __threadfence();
+    // single thread: the slice covers the whole ring (no block sync needed
+    // because gid 0 of a 1-thread group owns every element)
+    const gcq::gwf::cfg c = gcq::gwf::load_cfg(h);
+    for (uint32_t i = 0; i < c.slots(); ++i) c.entry[i] = gcq::gwf::entry::INIT;
+    if (full)
+        for (uint32_t i = 0; i < N_PARAM; ++i) {
+            const uint64_t t = (uint64_t)c.slots() + i;
+            c.entry[c.slot_of(t)] = gcq::gwf::entry::pack(0xFF, c.cycle_of(t), true, true, i);
+        }
+    for (uint32_t i = 0; i < c.max_threads; ++i) {
+        gcq::gwf::record* r = &c.rec[i];
+        r->seq1 = 1; r->enqueue = 0; r->pending = 0; r->index = 0;
+        r->localTail = 0; r->initTail = 0; r->localHead = 0; r->initHead = 0; r->seq2 = 0;
+        r->p2_seq1 = 1; r->p2_local = 0; r->p2_cnt = 0; r->p2_seq2 = 0;
+        c.help[i].nextCheck = (int32_t)c.help_delay;
+        c.help[i].nextTid = i;
+    }
+    h->Head = c.pack_global(c.slots(), c.null_tid());
+    h->Tail = c.pack_global(full ? c.slots() + N_PARAM : c.slots(), c.null_tid());
+    h->Threshold = full ? c.threshold_max() : -1;
+    __threadfence();
+}
+template <typename Config, uint32_t N_PARAM>
+__device__ void wf_mpmc_init(wf_mpmc_t<Config, N_PARAM>* q) {
+    wf_init(&q->aq, false);
+    wf_init(&q->fq, true);
+}
+template <typename Config, uint32_t N_PARAM>
+__device__ __forceinline__ void Enqueue_wf(wf_t<Config, N_PARAM>* q, uint32_t index) {
+    gcq::gwf::enqueue(&q->hdr, index, wf_tid());
+}
+template <typename Config, uint32_t N_PARAM>
+__device__ __forceinline__ uint32_t Dequeue_wf(wf_t<Config, N_PARAM>* q) {
+    return gcq::gwf::dequeue(&q->hdr, wf_tid());
+}
+template <typename Config, uint32_t N_PARAM>
+__device__ __forceinline__ bool Enqueue_Ptr(wf_mpmc_t<Config, N_PARAM>* q, uint64_t value) {
+    const uint32_t tid = wf_tid();
+    const uint32_t idx = gcq::gwf::dequeue(&q->fq.hdr, tid);
+    if (idx == gcq::gwf::BOT) return false;
+    gcq::st_rlx((gcq::u64a*)&q->data[idx], value);
+    gcq::gwf::enqueue(&q->aq.hdr, idx, tid);
+    return true;
+}
+template <typename Config, uint32_t N_PARAM>
+__device__ __forceinline__ bool Dequeue_Ptr(wf_mpmc_t<Config, N_PARAM>* q, uint64_t* out) {
+    const uint32_t tid = wf_tid();
+    const uint32_t idx = gcq::gwf::dequeue(&q->aq.hdr, tid);
+    if (idx == gcq::gwf::BOT) return false;
+    *out = gcq::ld_rlx((const gcq::u64a*)&q->data[idx]);
+    gcq::gwf::enqueue(&q->fq.hdr, idx, tid);
+    return true;
+}

@@ -1,0 +1,338 @@
+// WFQ-YMC for sm_103a: the GPU adaptation of Yang & Mellor-Crummey's wait-free
+// queue in wfqueue_hip_opt.hpp (segmented cells, per-thread handles with enqueue
+// and dequeue requests, fast path / slow path / helping, preallocated cell pool
+// without reclamation).
+//
+// Kept from the reference: sentinels BOTTOM=0, TOP=~0, RETRY=~0-1, EMPTY=0
+// (:41-58); request state = pending<<63 | id (:124-129); find_cell over a flat
+// preallocated pool returning null when exhausted (:208-237); enq_fast/enq_slow/
+// enq_commit (:259-318); help_enq (:320-413); deq_fast/help_deq/deq_slow
+// (:416-524); the patience loops of wf_enqueue/wf_dequeue (:527-555); the pool size
+// threads * (3 * ops + 128) cells plus 8 spare segments (:594-599).
+// Changed for GB300:
+//   * a cell is 32 bytes {val, enq, deq, pad}, one sector, instead of 24;
+//   * cell.enq / cell.deq name a request by handle index (2 + h; 0 null, 1 top)
+//     rather than by pointer;
+//   * find_cell no longer does atomicMax(active_segments) on every access (:229-232):
+//     every cell an operation touches is below max(T, H), which the reset kernel
+//     reads instead;
+//   * advance_end is one atom.max instead of a CAS loop (:192-199);
+//   * the T and H tickets are warp-aggregated;
+//   * request publication is release/acquire; loops are bounded.
+#pragma once
+
+#include <stdint.h>
+#include "gcq_atomics.cuh"
+
+#ifndef WF_SEGMENT_SIZE
+#define WF_SEGMENT_SIZE 1024u
+#endif
+#ifndef WF_PATIENCE
+#define WF_PATIENCE 16
+#endif
+#ifndef WF_PREALLOC_OPS_PER_THREAD
+#define WF_PREALLOC_OPS_PER_THREAD 512
+#endif
+#ifndef WF_SEGMENT_SAFETY
+#define WF_SEGMENT_SAFETY 8
+#endif
+#ifndef WF_EMPTY
+#define WF_EMPTY 0ull
+#endif
+
+namespace gcq {
+namespace ymc {
+
+constexpr uint64_t BOTTOM = 0ULL;
+constexpr uint64_t TOP = ~0ULL;
+constexpr uint64_t EMPTY = WF_EMPTY;
+constexpr uint64_t RETRY = ~0ULL - 1;
+constexpr uint64_t REQ_NULL = 0, REQ_TOP = 1;   // cell.enq / cell.deq markers
+
+__host__ __device__ __forceinline__ uint64_t pack_state(int pending, uint64_t low63) {
+    return ((uint64_t)pending << 63) | (low63 & ((1ULL << 63) - 1));
+}
+__host__ __device__ __forceinline__ int state_pending(uint64_t s) { return (int)(s >> 63); }
+__host__ __device__ __forceinline__ uint64_t state_low(uint64_t s) { return s & ((1ULL << 63) - 1); }
+
+struct alignas(32) cell {
+    u64a val;   // data, BOTTOM or TOP
+    u64a enq;   // REQ_NULL, REQ_TOP or 2 + handle index
+    u64a deq;
+    u64a _pad;
+};
+
+// Per-thread handle (wfqueue_hip_opt.hpp:161-178).  The request words are shared;
+// the cursors are private to the owning thread.
+struct alignas(64) handle {
+    u64a enq_val, enq_state;   // enqueue request
+    u64a deq_id, deq_state;    // dequeue request
+    uint32_t next;             // next handle in the ring (read-only after init)
+    uint32_t enq_peer, deq_peer;
+    uint32_t _pad;
+    uint64_t enq_id_last;
+};
+
+struct alignas(128) queue {
+    u64a T;
+    char _pad0[120];
+    u64a H;
+    char _pad1[120];
+    cell* cells;
+    handle* handles;
+    u32a* err;
+    uint64_t cap_cells;   // pool size (cells)
+    uint32_t nhandles;
+    uint32_t patience;
+    char _pad2[88];
+};
+
+struct ctx {
+    queue* q;
+    cell* cells;
+    handle* hs;
+    u32a* err;
+    uint64_t cap;
+    __device__ __forceinline__ cell* find_cell(uint64_t id) const {
+        if (id >= cap) { raise_error(err, ERR_POOL); return nullptr; }
+        return &cells[id];
+    }
+    __device__ __forceinline__ uint64_t req_of(uint32_t h) const { return 2ULL + h; }
+};
+
+__device__ __forceinline__ ctx load_ctx(queue* q) {
+    ctx c;
+    c.q = q; c.cells = q->cells; c.hs = q->handles; c.err = q->err; c.cap = q->cap_cells;
+    return c;
+}
+
+// wf_init_kernel (:571-591) and the pool clearing of wf_clear_pool_kernel (:646-663),
+// as one grid-stride slice over `ncells` cells and the handles.
+__device__ inline void init_slice(queue* q, uint64_t ncells, uint64_t gid, uint64_t nthreads) {
+    for (uint64_t i = gid; i < ncells; i += nthreads) {
+        cell* c = &q->cells[i];
+        c->val = BOTTOM; c->enq = REQ_NULL; c->deq = REQ_NULL; c->_pad = 0;
+    }
+    const uint32_t n = q->nhandles;
+    for (uint64_t i = gid; i < n; i += nthreads) {
+        handle* h = &q->handles[i];
+        h->enq_val = 0; h->enq_state = pack_state(0, 0);
+        h->deq_id = 0; h->deq_state = pack_state(0, 0);
+        h->next = (uint32_t)((i + 1) % n);
+        h->enq_peer = h->next;
+        h->deq_peer = h->next;
+        h->enq_id_last = 0;
+    }
+    if (gid == 0) { q->T = 0; q->H = 0; }
+}
+
+// advance_end_for_linearizability (:192-199): monotone raise of T or H.
+__device__ __forceinline__ void advance_end(u64a* e, uint64_t cid) { fetch_max(e, cid); }
+
+__device__ __forceinline__ bool try_to_claim_req(u64a* state, uint64_t expect_id, uint64_t cell_id) {
+    return cas_ok(state, pack_state(1, expect_id), pack_state(0, cell_id));
+}
+
+__device__ __forceinline__ void enq_commit(const ctx& x, cell* c, uint64_t v, uint64_t cid) {
+    advance_end(&x.q->T, cid + 1);
+    exchange(&c->val, v);
+}
+
+__device__ __forceinline__ bool enq_fast(const ctx& x, uint64_t v, uint64_t* cid) {
+    const uint64_t i = warp_fetch_add(&x.q->T, 1);
+    cell* c = x.find_cell(i);
+    if (c && cas_ok(&c->val, BOTTOM, v)) return true;
+    *cid = i;
+    return false;
+}
+
+__device__ inline bool enq_slow(const ctx& x, uint32_t hid, uint64_t v, uint64_t cell_id) {
+    handle* h = &x.hs[hid];
+    st_rlx(&h->enq_val, v);
+    st_rel(&h->enq_state, pack_state(1, cell_id));
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        const uint64_t i = fetch_add(&x.q->T, 1);
+        cell* c = x.find_cell(i);
+        if (!c) break;
+        if (cas(&c->enq, REQ_NULL, x.req_of(hid)) == REQ_NULL) {
+            const uint64_t cur = ld_acq(&c->val);
+            if (cur == BOTTOM || cur == TOP) {
+                try_to_claim_req(&h->enq_state, cell_id, i);
+                break;
+            }
+        }
+        if (!state_pending(ld_acq(&h->enq_state))) break;
+    }
+    const uint64_t final_id = state_low(ld_acq(&h->enq_state));
+    cell* d = x.find_cell(final_id);
+    if (d) {
+        if (ld_acq(&d->val) == TOP) enq_commit(x, d, v, final_id);
+        return true;
+    }
+    return false;   // pool exhausted: the value was dropped, as in the reference
+}
+
+__device__ inline uint64_t help_enq(const ctx& x, uint32_t hid, cell* c, uint64_t i) {
+    handle* h = &x.hs[hid];
+    const uint64_t old = cas(&c->val, BOTTOM, TOP);
+    if (old != BOTTOM && old != TOP) return old;
+    uint64_t ce = ld_acq(&c->enq);
+    if (ce == REQ_NULL) {
+        uint32_t p = h->enq_peer;
+        uint64_t s = ld_acq(&x.hs[p].enq_state);
+        uint64_t rid = state_low(s);
+        int pend = state_pending(s);
+        if (h->enq_id_last != 0 && h->enq_id_last != rid) {
+            h->enq_id_last = 0;
+            p = x.hs[p].next;
+            h->enq_peer = p;
+            s = ld_acq(&x.hs[p].enq_state);
+            rid = state_low(s);
+            pend = state_pending(s);
+        }
+        if (pend && rid > 0 && rid <= i) {
+            const uint64_t prev = cas(&c->enq, REQ_NULL, x.req_of(p));
+            if (prev != REQ_NULL && prev != x.req_of(p)) {
+                ce = prev;
+                h->enq_id_last = rid;
+            } else {
+                ce = x.req_of(p);
+                h->enq_id_last = 0;
+                h->enq_peer = x.hs[p].next;
+            }
+        } else {
+            h->enq_id_last = 0;
+            h->enq_peer = x.hs[p].next;
+        }
+        if (ce == REQ_NULL) {
+            const uint64_t prev = cas(&c->enq, REQ_NULL, REQ_TOP);
+            ce = (prev == REQ_NULL) ? REQ_TOP : prev;
+        }
+    }
+    if (ce == REQ_TOP) return ld_acq(&x.q->T) <= i ? EMPTY : RETRY;
+    handle* rh = &x.hs[ce - 2];
+    const uint64_t s = ld_acq(&rh->enq_state);
+    const int pend = state_pending(s);
+    const uint64_t rid = state_low(s);
+    const uint64_t v = ld_rlx(&rh->enq_val);
+    if (!pend) {
+        if (rid == i) {
+            if (ld_acq(&c->val) == TOP) enq_commit(x, c, v, i);
+            return ld_acq(&c->val);
+        }
+        return ld_acq(&x.q->T) <= i ? EMPTY : RETRY;
+    }
+    if (rid > i) return ld_acq(&x.q->T) <= i ? EMPTY : RETRY;
+    if (try_to_claim_req(&rh->enq_state, rid, i) || ld_acq(&rh->enq_state) == pack_state(0, i)) {
+        if (ld_acq(&c->val) == TOP) enq_commit(x, c, v, i);
+    }
+    return ld_acq(&c->val);
+}
+
+__device__ __forceinline__ uint64_t deq_fast(const ctx& x, uint32_t hid, uint64_t* id_out) {
+    const uint64_t i = warp_fetch_add(&x.q->H, 1);
+    cell* c = x.find_cell(i);
+    if (!c) { *id_out = i; return EMPTY; }
+    const uint64_t v = help_enq(x, hid, c, i);
+    if (v == EMPTY) return EMPTY;
+    if (v != TOP && v != RETRY && cas(&c->deq, REQ_NULL, REQ_TOP) == REQ_NULL) return v;
+    *id_out = i;
+    return RETRY;
+}
+
+__device__ inline void help_deq(const ctx& x, uint32_t hid, uint32_t helpee) {
+    handle* r = &x.hs[helpee];
+    uint64_t s = ld_acq(&r->deq_state);
+    const uint64_t id = ld_rlx(&r->deq_id);
+    if (!state_pending(s) || state_low(s) < id) return;
+    uint64_t prior = id, i = id, cand = 0;
+    for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
+        s = ld_acq(&r->deq_state);
+        if (!state_pending(s) || ld_rlx(&r->deq_id) != id) return;
+        while (!cand && state_pending(s) && state_low(s) == prior) {
+            cell* c = x.find_cell(++i);
+            if (!c) break;
+            advance_end(&x.q->H, i + 1);
+            const uint64_t v = help_enq(x, hid, c, i);
+            if (v == EMPTY || (v != TOP && v != RETRY && ld_acq(&c->deq) == REQ_NULL)) {
+                cand = i;
+                break;
+            }
+            s = ld_acq(&r->deq_state);
+            if (!state_pending(s) || ld_rlx(&r->deq_id) != id) return;
+        }
+        if (cand) {
+            cas(&r->deq_state, pack_state(1, prior), pack_state(1, cand));
+            cand = 0;
+        }
+        s = ld_acq(&r->deq_state);
+        if (!state_pending(s) || ld_rlx(&r->deq_id) != id) return;
+        const uint64_t aidx = state_low(s);
+        cell* c = x.find_cell(aidx);
+        if (!c) return;
+        const uint64_t cur_deq = ld_acq(&c->deq);
+        if (ld_acq(&c->val) == TOP || cas(&c->deq, REQ_NULL, x.req_of(helpee)) == REQ_NULL ||
+            cur_deq == x.req_of(helpee)) {
+            cas(&r->deq_state, s, pack_state(0, aidx));
+            return;
+        }
+        prior = aidx;
+        if (aidx >= i) i = aidx;
+    }
+    raise_error(x.err, ERR_SPIN);
+}
+
+__device__ inline uint64_t deq_slow(const ctx& x, uint32_t hid, uint64_t cid) {
+    handle* h = &x.hs[hid];
+    st_rlx(&h->deq_id, cid);
+    st_rel(&h->deq_state, pack_state(1, cid));
+    help_deq(x, hid, hid);
+    const uint64_t idx = state_low(ld_acq(&h->deq_state));
+    cell* c = x.find_cell(idx);
+    if (!c) {
+        advance_end(&x.q->H, idx + 1);
+        return EMPTY;
+    }
+    const uint64_t v = ld_acq(&c->val);
+    advance_end(&x.q->H, idx + 1);
+    return v == TOP ? EMPTY : v;
+}
+
+// wf_enqueue, :527-536.  `v` must not be 0, ~0 or ~0-1.
+__device__ inline bool enqueue(queue* q, uint32_t hid, uint64_t v) {
+    const ctx x = load_ctx(q);
+    const int patience = (int)q->patience;
+    for (int p = patience; p >= 0; --p) {
+        uint64_t cid = 0;
+        if (enq_fast(x, v, &cid)) return true;
+        if (p == 0) return enq_slow(x, hid, v, cid);
+    }
+    return false;
+}
+
+// wf_dequeue, :538-555.  Returns the value or EMPTY.
+__device__ inline uint64_t dequeue(queue* q, uint32_t hid) {
+    const ctx x = load_ctx(q);
+    const int patience = (int)q->patience;
+    uint64_t v = RETRY, cid = 0;
+    for (int p = patience; p >= 0; --p) {
+        v = deq_fast(x, hid, &cid);
+        if (v != RETRY) break;
+    }
+    if (v == RETRY) v = deq_slow(x, hid, cid);
+    if (v != EMPTY) {
+        handle* h = &x.hs[hid];
+        help_deq(x, hid, h->deq_peer);
+        h->deq_peer = x.hs[h->deq_peer].next;
+    }
+    return v;
+}
+
+}  // namespace ymc
+}  // namespace gcq
+
+// Reference-named device API (wfqueue_hip_opt.hpp:527-555).  The handle argument
+// is the caller's handle index in this build.
+typedef gcq::ymc::queue wf_queue;
+__device__ __forceinline__ bool wf_enqueue(wf_queue* q, uint32_t h, uint64_t value) { return gcq::ymc::enqueue(q, h, value); }
+__device__ __forceinline__ uint64_t wf_dequeue(wf_queue* q, uint32_t h) { return gcq::ymc::dequeue(q, h); }

@@ -1,0 +1,1195 @@
+// CPU restatements of gCQ's four queues: test infrastructure (the oracle and the
+// timed CPU baseline), never the product path.
+//
+// Each queue follows the reference algorithm step for step, with std::atomic
+// (sequentially consistent) in place of the HIP device atomics the reference
+// assumes to be sequentially consistent (gwf_ring.hpp:15-17).  Warp-aggregated
+// ticket fetch-and-add becomes one fetch-and-add per thread, which is what the
+// reference's batched helper reduces to for a single lane (gwf_ring.hpp:220-222,
+// glf_queue.hpp:392-412).  Host threads stand in for GPU threads; the thread
+// index passed to each call plays the part of wf_tid() (gwf_ring.hpp:53-63).
+//
+//   G-WFQ  gwf_queue.hpp:31-345 (types), gwf_ring.hpp:229-298 (init),
+//          :309-371 (consume/finalize/catchup), :382-472 (fast path),
+//          :486-639 (phase-2 records, cooperative FAA), :650-802 (slow path),
+//          :808-861 (helping), :1234-1356 (Enqueue_wf/Dequeue_wf),
+//          :1362-1380 (Enqueue_Ptr/Dequeue_Ptr)
+//   G-LFQ  glf_queue.hpp:44-138 (layout), :418-440 (init), :447-455 (catchup),
+//          :467-582 (enqueue/dequeue/indirection)
+//   YMC    wfqueue_hip_opt.hpp:124-189 (layout), :192-237 (find_cell),
+//          :248-318 (enqueue), :320-413 (help_enq), :416-524 (dequeue),
+//          :527-555 (public API), :571-644 (init)
+//   SFQ    sfqueue_hip.hpp:13-66 (layout, ids), sfqueue_hip.cpp:31-128 (ops),
+//          :134-144 (u64 wrapper)
+//
+// Runners at the end drive them like the reference harnesses:
+//   history      correctness/history.cpp:188-227 with the logical clock of
+//                correctness/wf_linlog.hpp:25-45
+//   throughput   throughout_bench.cpp:810-882 (balanced and split kernels)
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <thread>
+#include <vector>
+
+namespace {
+
+using u32 = uint32_t;
+using u64 = uint64_t;
+using clk = std::chrono::steady_clock;
+
+enum Kind { GWFQ = 0, GLFQ = 1, WFQ = 2, SFQ = 3 };
+
+static inline void cpu_relax() { std::this_thread::yield(); }
+
+// =============================================================================
+// G-WFQ
+// =============================================================================
+namespace gwf {
+
+constexpr u32 CYCLE_MASK = 0xFF, HALF_CYCLE = 0x80;
+constexpr int NOTE_SHIFT = 56, CYCLE_SHIFT = 48, SAFE_SHIFT = 47, ENQ_SHIFT = 46;
+constexpr u64 SAFE_BIT = 1ULL << SAFE_SHIFT, ENQ_BIT = 1ULL << ENQ_SHIFT;
+constexpr u32 BOT = 0xFFFFFFFEu, BOT_C = 0xFFFFFFFFu;
+constexpr u64 CONSUME_MASK = ENQ_BIT | (u64)BOT_C;
+constexpr u64 INIT = (0xFFULL << NOTE_SHIFT) | SAFE_BIT | ENQ_BIT | BOT;
+constexpr u64 FIN = 1, INC = 2, CNT_MASK = ~3ULL;
+
+static inline u32 note(u64 e) { return (u32)((e >> NOTE_SHIFT) & CYCLE_MASK); }
+static inline u32 cyc(u64 e) { return (u32)((e >> CYCLE_SHIFT) & CYCLE_MASK); }
+static inline bool safe(u64 e) { return (e >> SAFE_SHIFT) & 1; }
+static inline bool enq(u64 e) { return (e >> ENQ_SHIFT) & 1; }
+static inline u32 idx(u64 e) { return (u32)e; }
+static inline u64 pack(u32 n, u32 c, bool s, bool q, u32 i) {
+    return ((u64)(n & CYCLE_MASK) << NOTE_SHIFT) | ((u64)(c & CYCLE_MASK) << CYCLE_SHIFT) |
+           ((u64)s << SAFE_SHIFT) | ((u64)q << ENQ_SHIFT) | (u64)i;
+}
+static inline int ccmp(u32 a, u32 b) {
+    u32 d = (a - b) & CYCLE_MASK;
+    return d == 0 ? 0 : (d < HALF_CYCLE ? 1 : -1);
+}
+
+struct Rec {
+    // phase-2 record (gwf_queue.hpp:242-247)
+    std::atomic<u32> p2_seq1{1};
+    std::atomic<u64> p2_local{0};   // address of the victim's localTail/localHead
+    std::atomic<u64> p2_cnt{0};
+    std::atomic<u32> p2_seq2{0};
+    // help request (gwf_queue.hpp:272-286)
+    std::atomic<u32> seq1{1}, enqueue{0}, pending{0};
+    std::atomic<u64> localTail{0}, initTail{0}, localHead{0}, initHead{0};
+    std::atomic<u32> index{0}, seq2{0};
+    // private countdown (gwf_queue.hpp:260-261)
+    int32_t nextCheck = 64;
+    u32 nextTid = 0;
+    char pad[8];
+};
+
+struct Knobs { int help_delay = 64, enq_patience = 128, deq_patience = 256; };
+
+struct Ring {
+    alignas(128) std::atomic<u64> Tail{0};
+    alignas(128) std::atomic<u64> Head{0};
+    alignas(128) std::atomic<int32_t> Threshold{-1};
+    u32 n = 0, slots = 0, max_threads = 0;
+    int thr_bits = 0;
+    u64 null_tid = 0, cinc = 0;
+    Knobs k;
+    std::unique_ptr<std::atomic<u64>[]> Entry;
+    std::unique_ptr<Rec[]> Record;
+
+    u64 packg(u64 cnt, u32 t) const { return (cnt << thr_bits) | ((u64)t & null_tid); }
+    u64 cnt_of(u64 g) const { return g >> thr_bits; }
+    u32 tid_of(u64 g) const { return (u32)(g & null_tid); }
+    u32 cycle_of(u64 t) const { return (u32)((t / slots) & CYCLE_MASK); }
+    u32 slot_of(u64 t) const { return (u32)(t & (slots - 1)); }
+    int32_t thr_max() const { return 3 * (int32_t)n - 1; }
+
+    void init(u32 n_, u32 max_threads_, int thr_bits_, Knobs kn) {
+        n = n_; slots = 2 * n_; max_threads = max_threads_; thr_bits = thr_bits_; k = kn;
+        null_tid = (1ULL << thr_bits) - 1;
+        cinc = 1ULL << thr_bits;
+        Entry.reset(new std::atomic<u64>[slots]);
+        Record.reset(new Rec[max_threads]);
+        reset(false);
+    }
+    void reset(bool full) {
+        Tail = packg(slots, (u32)null_tid);
+        Head = packg(slots, (u32)null_tid);
+        Threshold = -1;
+        for (u32 i = 0; i < slots; ++i) Entry[i].store(INIT);
+        for (u32 i = 0; i < max_threads; ++i) {
+            Rec& r = Record[i];
+            r.nextCheck = k.help_delay; r.nextTid = i;
+            r.p2_seq1 = 1; r.p2_local = 0; r.p2_cnt = 0; r.p2_seq2 = 0;
+            r.seq1 = 1; r.enqueue = 0; r.pending = 0;
+            r.localTail = 0; r.initTail = 0; r.localHead = 0; r.initHead = 0;
+            r.index = 0; r.seq2 = 0;
+        }
+        if (full) {  // gwf_ring.hpp:286-297
+            for (u32 i = 0; i < n; ++i) {
+                u64 t = (u64)slots + i;
+                Entry[slot_of(t)].store(pack(0xFF, cycle_of(t), true, true, i));
+            }
+            Tail = packg((u64)slots + n, (u32)null_tid);
+            Threshold = thr_max();
+        }
+    }
+
+    // ---- consume / finalize / catchup --------------------------------------
+    void finalize_request(u64 h_raw, u32 me) {
+        u64 hl = h_raw << 2;
+        u32 i = (me + 1) % max_threads;
+        while (i != me) {
+            u64 lt = Record[i].localTail.load();
+            if ((lt & CNT_MASK) == hl) {
+                u64 e = hl;
+                Record[i].localTail.compare_exchange_strong(e, hl | FIN);
+                return;
+            }
+            i = (i + 1) % max_threads;
+        }
+    }
+    void consume(u64 h_raw, u32 j, u64 e, u32 me) {
+        if (!enq(e)) finalize_request(h_raw, me);
+        Entry[j].fetch_or(CONSUME_MASK);
+    }
+    void catchup(u64 tail_raw, u64 head_raw) {
+        for (int i = 0; i < 32; ++i) {
+            u64 cur = Tail.load();
+            u64 cc = cnt_of(cur);
+            if (cc >= head_raw) break;
+            if (cc != tail_raw) {
+                tail_raw = cc;
+                head_raw = cnt_of(Head.load());
+                if (tail_raw >= head_raw) break;
+                continue;
+            }
+            u64 want = packg(head_raw, tid_of(cur));
+            if (Tail.compare_exchange_strong(cur, want)) break;
+            head_raw = cnt_of(Head.load());
+            tail_raw = cnt_of(Tail.load());
+            if (tail_raw >= head_raw) break;
+        }
+    }
+
+    // ---- fast path ---------------------------------------------------------
+    u64 try_enq(u32 index) {
+        u64 T = cnt_of(Tail.fetch_add(cinc));
+        u32 tc = cycle_of(T), j = slot_of(T);
+        u64 E = Entry[j].load();
+        for (;;) {
+            u32 ec = cyc(E), ei = idx(E);
+            if (ccmp(ec, tc) < 0 && (safe(E) || cnt_of(Head.load()) <= T) &&
+                (ei == BOT || ei == BOT_C)) {
+                u64 nw = pack(note(E), tc, true, true, index);
+                if (!Entry[j].compare_exchange_strong(E, nw)) continue;
+                if (Threshold.load() != thr_max()) Threshold.exchange(thr_max());
+                return 0;
+            }
+            return T;
+        }
+    }
+    u64 try_deq(u32* out, u32 me) {
+        u64 H = cnt_of(Head.fetch_add(cinc));
+        u32 hc = cycle_of(H), j = slot_of(H);
+        u64 E = Entry[j].load();
+        for (;;) {
+            u32 ec = cyc(E), ei = idx(E);
+            if (ccmp(ec, hc) == 0 && ei != BOT && ei != BOT_C) {
+                consume(H, j, E, me);
+                *out = ei;
+                return 0;
+            }
+            u64 nw = (ei == BOT || ei == BOT_C) ? pack(note(E), hc, safe(E), true, BOT)
+                                                : pack(note(E), ec, false, enq(E), ei);
+            if (ccmp(ec, hc) < 0) {
+                if (!Entry[j].compare_exchange_strong(E, nw)) continue;
+            }
+            break;
+        }
+        u64 T = cnt_of(Tail.load());
+        if (T <= H + 1) {
+            catchup(T, H + 1);
+            Threshold.fetch_sub(1);
+            *out = BOT;
+            return 0;
+        }
+        if (Threshold.fetch_sub(1) <= 0) { *out = BOT; return 0; }
+        return H;
+    }
+
+    // ---- cooperative fetch-and-add -----------------------------------------
+    void prepare_phase2(Rec& me, std::atomic<u64>* local, u64 cnt_local) {
+        u32 seq = me.p2_seq1.load() + 1;
+        me.p2_seq1.store(seq);
+        me.p2_local.store((u64)(uintptr_t)local);
+        me.p2_cnt.store(cnt_local);
+        me.p2_seq2.store(seq);
+    }
+    bool slow_faa(std::atomic<u64>* gp_, std::atomic<u64>* local, u64* v,
+                  std::atomic<int32_t>* thld, u32 me) {
+        Rec& mine = Record[me];
+        u64 cnt_local = 0, cnt_raw = 0;
+        bool ok = false;
+        do {
+            u64 lc = local->load();
+            if (lc & FIN) { *v = lc; return false; }
+            u64 gp = gp_->load();
+            u32 gt = tid_of(gp);
+            if (gt != (u32)null_tid) {
+                Rec& hr = Record[gt];
+                u32 seq = hr.p2_seq2.load();
+                auto* p2l = (std::atomic<u64>*)(uintptr_t)hr.p2_local.load();
+                u64 p2c = hr.p2_cnt.load();
+                u32 s1 = hr.p2_seq1.load();
+                if (s1 == seq && p2l) {
+                    u64 e = p2c | INC;
+                    p2l->compare_exchange_strong(e, p2c);
+                }
+                u64 clean = packg(cnt_of(gp), (u32)null_tid);
+                if (!gp_->compare_exchange_strong(gp, clean)) continue;
+                gp = clean;
+            }
+            cnt_raw = cnt_of(gp);
+            cnt_local = cnt_raw << 2;
+            u64 vc = *v;
+            if (!local->compare_exchange_strong(vc, cnt_local | INC)) {
+                *v = vc;
+                if (vc & FIN) return false;
+                if (!(vc & INC)) return true;
+                cnt_local = vc & CNT_MASK;
+                cnt_raw = cnt_local >> 2;
+            } else {
+                *v = cnt_local | INC;
+            }
+            prepare_phase2(mine, local, cnt_local);
+            u64 exp = packg(cnt_raw, (u32)null_tid);
+            ok = gp_->compare_exchange_strong(exp, packg(cnt_raw + 1, me));
+        } while (!ok);
+        if (thld) thld->fetch_sub(1);
+        u64 e = cnt_local | INC;
+        local->compare_exchange_strong(e, cnt_local);
+        u64 g = packg(cnt_raw + 1, me);
+        gp_->compare_exchange_strong(g, packg(cnt_raw + 1, (u32)null_tid));
+        *v = cnt_local;
+        return true;
+    }
+
+    // ---- slow path ---------------------------------------------------------
+    bool try_enq_slow(u64 T, u32 index, Rec& r) {
+        u32 tc = cycle_of(T), j = slot_of(T);
+        u64 P = Entry[j].load();
+        for (;;) {
+            u32 ec = cyc(P), en = note(P), ei = idx(P);
+            if (ccmp(ec, tc) < 0 && ccmp(en, tc) < 0) {
+                if ((!safe(P) && cnt_of(Head.load()) > T) || (ei != BOT && ei != BOT_C)) {
+                    u64 nn = pack(tc, ec, safe(P), enq(P), ei);
+                    if (!Entry[j].compare_exchange_strong(P, nn)) continue;
+                    return false;
+                }
+                u64 nn = pack(en, tc, true, false, index);
+                if (!Entry[j].compare_exchange_strong(P, nn)) continue;
+                u64 tl = T << 2;
+                if (r.localTail.compare_exchange_strong(tl, (T << 2) | FIN)) {
+                    u64 e0 = nn;
+                    Entry[j].compare_exchange_strong(e0, pack(en, tc, true, true, index));
+                }
+                if (Threshold.load() != thr_max()) Threshold.exchange(thr_max());
+                return true;
+            } else if (ccmp(ec, tc) != 0) {
+                return false;
+            }
+            return true;
+        }
+    }
+    bool try_deq_slow(u64 H, Rec& r) {
+        u32 hc = cycle_of(H), j = slot_of(H);
+        u64 P = Entry[j].load();
+        for (;;) {
+            u32 ec = cyc(P), en = note(P), ei = idx(P);
+            if (ccmp(ec, hc) == 0 && ei != BOT && ei != BOT_C) {
+                u64 hl = H << 2;
+                r.localHead.compare_exchange_strong(hl, (H << 2) | FIN);
+                return true;
+            }
+            u32 nnote = en;
+            u64 val = pack(nnote, hc, safe(P), true, BOT);
+            if (ei != BOT && ei != BOT_C) {
+                if (ccmp(ec, hc) < 0 && ccmp(en, hc) < 0) {
+                    u64 nn = pack(hc, ec, safe(P), enq(P), ei);
+                    if (!Entry[j].compare_exchange_strong(P, nn)) continue;
+                    nnote = hc;
+                }
+                val = pack(nnote, ec, false, enq(P), ei);
+            }
+            if (ccmp(ec, hc) < 0) {
+                if (!Entry[j].compare_exchange_strong(P, val)) continue;
+            }
+            break;
+        }
+        u64 T = cnt_of(Tail.load());
+        if (T <= H + 1) catchup(T, H + 1);
+        if (Threshold.load() < 0) {
+            u64 hl = H << 2;
+            r.localHead.compare_exchange_strong(hl, (H << 2) | FIN);
+            return true;
+        }
+        return false;
+    }
+    void enqueue_slow(u64 v, u32 index, Rec& r, u32 me) {
+        while (slow_faa(&Tail, &r.localTail, &v, nullptr, me))
+            if (try_enq_slow(v >> 2, index, r)) break;
+    }
+    void dequeue_slow(u64 v, Rec& r, u32 me) {
+        while (slow_faa(&Head, &r.localHead, &v, &Threshold, me))
+            if (try_deq_slow(v >> 2, r)) break;
+    }
+
+    // ---- helping -----------------------------------------------------------
+    void help_enqueue(Rec& t, u32 me) {
+        u32 seq = t.seq2.load();
+        u32 is_enq = t.enqueue.load();
+        u32 index = t.index.load();
+        u64 it = t.initTail.load();
+        if (is_enq && t.seq1.load() == seq) enqueue_slow(it, index, t, me);
+    }
+    void help_dequeue(Rec& t, u32 me) {
+        u32 seq = t.seq2.load();
+        u32 is_enq = t.enqueue.load();
+        u64 ih = t.initHead.load();
+        if (!is_enq && t.seq1.load() == seq) dequeue_slow(ih, t, me);
+    }
+    void help_threads(u32 me) {
+        Rec& r = Record[me];
+        if (--r.nextCheck != 0) return;
+        Rec& t = Record[r.nextTid];
+        if (t.pending.load()) {
+            if (t.enqueue.load()) help_enqueue(t, me);
+            else help_dequeue(t, me);
+        }
+        r.nextCheck = k.help_delay;
+        r.nextTid = (r.nextTid + 1) % max_threads;
+    }
+
+    // ---- top level ---------------------------------------------------------
+    void enqueue_wf(u32 index, u32 me) {
+        help_threads(me);
+        u64 tail = 0;
+        int count = k.enq_patience;
+        while (--count != 0) {
+            tail = try_enq(index);
+            if (tail == 0) return;
+        }
+        Rec& r = Record[me];
+        u32 seq = r.seq1.load();
+        r.localTail.store(tail << 2);
+        r.initTail.store(tail << 2);
+        r.index.store(index);
+        r.enqueue.store(1);
+        r.seq2.store(seq);
+        r.pending.store(1);
+        enqueue_slow(tail << 2, index, r, me);
+        r.pending.store(0);
+        r.seq1.store(seq + 1);
+    }
+    u32 dequeue_wf(u32 me) {
+        if (Threshold.load() < 0) return BOT;
+        help_threads(me);
+        u32 out = BOT;
+        u64 head = 0;
+        int count = k.deq_patience;
+        while (--count != 0) {
+            head = try_deq(&out, me);
+            if (head == 0) return out;
+        }
+        Rec& r = Record[me];
+        u32 seq = r.seq1.load();
+        r.localHead.store(head << 2);
+        r.initHead.store(head << 2);
+        r.enqueue.store(0);
+        r.seq2.store(seq);
+        r.pending.store(1);
+        dequeue_slow(head << 2, r, me);
+        r.pending.store(0);
+        r.seq1.store(seq + 1);
+        u64 hr = r.localHead.load() >> 2;
+        u32 j = slot_of(hr);
+        u64 E = Entry[j].load();
+        if (ccmp(cyc(E), cycle_of(hr)) == 0 && idx(E) != BOT && idx(E) != BOT_C) {
+            consume(hr, j, E, me);
+            return idx(E);
+        }
+        return BOT;
+    }
+};
+
+struct Mpmc {
+    Ring aq, fq;
+    std::unique_ptr<std::atomic<u64>[]> data;
+    u32 n = 0;
+    void init(u32 n_, u32 max_threads, int thr_bits, Knobs k) {
+        n = n_;
+        aq.init(n, max_threads, thr_bits, k);
+        fq.init(n, max_threads, thr_bits, k);
+        fq.reset(true);
+        data.reset(new std::atomic<u64>[n]);
+        for (u32 i = 0; i < n; ++i) data[i].store(0, std::memory_order_relaxed);
+    }
+    bool enqueue(u64 v, u32 me) {
+        u32 i = fq.dequeue_wf(me);
+        if (i == BOT) return false;
+        data[i].store(v, std::memory_order_relaxed);
+        aq.enqueue_wf(i, me);
+        return true;
+    }
+    bool dequeue(u64* out, u32 me) {
+        u32 i = aq.dequeue_wf(me);
+        if (i == BOT) return false;
+        *out = data[i].load(std::memory_order_relaxed);
+        fq.enqueue_wf(i, me);
+        return true;
+    }
+};
+
+}  // namespace gwf
+
+// =============================================================================
+// G-LFQ
+// =============================================================================
+namespace glf {
+
+constexpr u32 CYCLE_MASK = 0xFF, HALF = 0x80;
+constexpr u32 BOT = 0xFFFFFFFEu, BOT_C = 0xFFFFFFFFu;
+constexpr u64 SAFE_BIT = 1ULL << 47;
+constexpr u64 INIT = SAFE_BIT | BOT;
+constexpr u32 PER_LINE = 8;  // 64-byte lines of 8-byte entries (glf_queue.hpp:50-51)
+
+static inline u32 cyc(u64 e) { return (u32)((e >> 48) & CYCLE_MASK); }
+static inline bool safe(u64 e) { return (e >> 47) & 1; }
+static inline u32 idx(u64 e) { return (u32)e; }
+static inline u64 pack(u32 c, bool s, u32 i) { return ((u64)(c & CYCLE_MASK) << 48) | ((u64)s << 47) | (u64)i; }
+static inline int ccmp(u32 a, u32 b) { u32 d = (a - b) & CYCLE_MASK; return d == 0 ? 0 : d < HALF ? 1 : -1; }
+
+struct Ring {
+    alignas(128) std::atomic<u64> Tail{0};
+    alignas(128) std::atomic<u64> Head{0};
+    alignas(128) std::atomic<int32_t> Threshold{-1};
+    u32 n = 0, slots = 0;
+    std::unique_ptr<std::atomic<u64>[]> Entry;
+    u32 cycle_of(u64 t) const { return (u32)((t / slots) & CYCLE_MASK); }
+    u32 remap(u64 t) const {
+        u32 p = (u32)(t & (slots - 1));
+        return (p & (PER_LINE - 1)) * (slots / PER_LINE) + p / PER_LINE;
+    }
+    int32_t thr_max() const { return 3 * (int32_t)n - 1; }
+    void init(u32 n_, bool full) {
+        n = n_; slots = 2 * n;
+        Entry.reset(new std::atomic<u64>[slots]);
+        Tail = slots; Head = slots; Threshold = -1;
+        for (u32 i = 0; i < slots; ++i) Entry[i].store(INIT);
+        if (full) {
+            for (u32 i = 0; i < n; ++i) {
+                u64 t = (u64)slots + i;
+                Entry[remap(t)].store(pack(cycle_of(t), true, i));
+            }
+            Tail = (u64)slots + n;
+            Threshold = thr_max();
+        }
+    }
+    void catchup(u64 tail, u64 head) {
+        for (int i = 0; i < 32; ++i) {
+            if (Tail.compare_exchange_strong(tail, head)) break;
+            head = Head.load();
+            tail = Tail.load();
+            if (tail >= head) break;
+        }
+    }
+    void enqueue(u32 index) {
+        for (;;) {
+            u64 T = Tail.fetch_add(1);
+            u32 tc = cycle_of(T), j = remap(T);
+            u64 E = Entry[j].load();
+            for (;;) {
+                u32 ec = cyc(E), ei = idx(E);
+                if (ccmp(ec, tc) < 0 && (safe(E) || Head.load() <= T) && (ei == BOT || ei == BOT_C)) {
+                    if (!Entry[j].compare_exchange_strong(E, pack(tc, true, index))) continue;
+                    if (Threshold.load() != thr_max()) Threshold.exchange(thr_max());
+                    return;
+                }
+                break;
+            }
+        }
+    }
+    u32 dequeue() {
+        if (Threshold.load() < 0) return BOT;
+        for (;;) {
+            u64 H = Head.fetch_add(1);
+            u32 hc = cycle_of(H), j = remap(H);
+            u64 E = Entry[j].load();
+            for (;;) {
+                u32 ec = cyc(E), ei = idx(E);
+                if (ccmp(ec, hc) == 0 && ei != BOT && ei != BOT_C) {
+                    Entry[j].fetch_or((u64)BOT_C);
+                    return ei;
+                }
+                u64 nw = (ei == BOT || ei == BOT_C) ? pack(hc, safe(E), BOT) : pack(ec, false, ei);
+                if (ccmp(ec, hc) < 0) {
+                    if (!Entry[j].compare_exchange_strong(E, nw)) continue;
+                }
+                break;
+            }
+            u64 T = Tail.load();
+            if (T <= H + 1) {
+                catchup(T, H + 1);
+                Threshold.fetch_sub(1);
+                return BOT;
+            }
+            if (Threshold.fetch_sub(1) <= 0) return BOT;
+        }
+    }
+};
+
+struct Mpmc {
+    Ring aq, fq;
+    std::unique_ptr<std::atomic<u64>[]> data;
+    void init(u32 n) {
+        aq.init(n, false);
+        fq.init(n, true);
+        data.reset(new std::atomic<u64>[n]);
+        for (u32 i = 0; i < n; ++i) data[i].store(0, std::memory_order_relaxed);
+    }
+    bool enqueue(u64 v) {
+        u32 i = fq.dequeue();
+        if (i == BOT) return false;
+        data[i].store(v, std::memory_order_relaxed);
+        aq.enqueue(i);
+        return true;
+    }
+    bool dequeue(u64* out) {
+        u32 i = aq.dequeue();
+        if (i == BOT) return false;
+        *out = data[i].load(std::memory_order_relaxed);
+        fq.enqueue(i);
+        return true;
+    }
+};
+
+}  // namespace glf
+
+// =============================================================================
+// SFQ (Scogland-Feng ticket queue)
+// =============================================================================
+namespace sfq {
+
+enum { SUCCESS = 0, BUSY = 1, CLOSED = 2, TIMEDOUT = 3 };
+
+struct Queue {
+    alignas(128) std::atomic<u32> head{0};
+    alignas(128) std::atomic<u32> tail{0};
+    alignas(128) std::atomic<u32> closed{0};
+    u32 L = 0, max_id = 0;
+    std::unique_ptr<std::atomic<u32>[]> items, ids;
+    double timeout_s = 10.0;
+    void init(u32 len) {
+        L = len;
+        max_id = 2u * ((UINT32_MAX / L) + 1u);   // sfqueue_hip.hpp:39
+        items.reset(new std::atomic<u32>[L]);
+        ids.reset(new std::atomic<u32>[L]);
+        for (u32 i = 0; i < L; ++i) { items[i].store(0); ids[i].store(0); }
+        head = 0; tail = 0; closed = 0;
+    }
+    u32 get_id(u32 t) const { return (t / L) * 2u; }   // sfqueue_hip.hpp:35
+    u32 next_id(u32 id) const { u32 n = id + 1; return n == max_id ? 0u : n; }
+    bool wait_id(u32 target, u32 id, clk::time_point t0) {
+        while (ids[target].load() != id) {
+            if (closed.load()) return false;
+            cpu_relax();
+            if (std::chrono::duration<double>(clk::now() - t0).count() > timeout_s) return false;
+        }
+        return true;
+    }
+    int enqueue_blocking(u32 item) {
+        if (closed.load()) return CLOSED;
+        u32 t = tail.fetch_add(1);
+        u32 target = t % L, id = get_id(t);
+        if (!wait_id(target, id, clk::now())) return closed.load() ? CLOSED : TIMEDOUT;
+        items[target].store(item);
+        ids[target].store(next_id(id));
+        return SUCCESS;
+    }
+    int dequeue_blocking(u32* out) {
+        if (closed.load()) return CLOSED;
+        u32 t = head.fetch_add(1);
+        u32 target = t % L, id = get_id(t) + 1u;
+        if (!wait_id(target, id, clk::now())) return closed.load() ? CLOSED : TIMEDOUT;
+        *out = items[target].load();
+        ids[target].store(next_id(id));
+        return SUCCESS;
+    }
+    int enqueue_nb(u32 item) {
+        if (closed.load()) return CLOSED;
+        u32 t = tail.load();
+        u32 target = t % L, id = get_id(t);
+        if (ids[target].load() != id) return BUSY;
+        if (!tail.compare_exchange_strong(t, t + 1)) return BUSY;
+        items[target].store(item);
+        ids[target].store(next_id(id));
+        return SUCCESS;
+    }
+    int dequeue_nb(u32* out) {
+        if (closed.load()) return CLOSED;
+        u32 t = head.load();
+        u32 target = t % L, id = get_id(t) + 1u;
+        if (ids[target].load() != id) return BUSY;
+        if (!head.compare_exchange_strong(t, t + 1)) return BUSY;
+        *out = items[target].load();
+        ids[target].store(next_id(id));
+        return SUCCESS;
+    }
+};
+
+}  // namespace sfq
+
+// =============================================================================
+// WFQ-YMC (Yang & Mellor-Crummey, GPU adaptation with a preallocated pool)
+// =============================================================================
+namespace ymc {
+
+constexpr u64 BOTTOM = 0, TOP = ~0ULL, EMPTY = 0, RETRY = ~0ULL - 1;
+constexpr u64 NUL = 0, TOPP = 1;
+constexpr int SEG = 1024;
+
+static inline u64 pst(int p, u64 low) { return ((u64)p << 63) | (low & ((1ULL << 63) - 1)); }
+static inline int pend(u64 s) { return (int)(s >> 63); }
+static inline u64 low(u64 s) { return s & ((1ULL << 63) - 1); }
+
+struct EnqReq { std::atomic<u64> val{0}, state{0}; };
+struct DeqReq { std::atomic<u64> id{0}, state{0}; };
+struct Cell { std::atomic<u64> val{0}; std::atomic<u64> enq{0}; std::atomic<u64> deq{0}; };
+
+struct Handle {
+    Handle* next = nullptr;
+    EnqReq enq_req;
+    Handle* enq_peer = nullptr;
+    u64 enq_id_last = 0;
+    DeqReq deq_req;
+    Handle* deq_peer = nullptr;
+};
+
+struct Queue {
+    alignas(128) std::atomic<u64> T{0};
+    alignas(128) std::atomic<u64> H{0};
+    std::unique_ptr<Cell[]> cells;
+    u64 cap_cells = 0;
+    int patience = 16;
+    std::unique_ptr<Handle[]> handles;
+    int nthreads = 0;
+
+    void init(int threads, int ops_per_thread) {
+        // wfqueue_hip_opt.hpp:595-599: threads * (3*ops + 128) cells, plus 8 spare segments
+        u64 per = (u64)(3 * ops_per_thread + 128);
+        u64 total = (u64)threads * per;
+        u64 segs = (total + SEG - 1) / SEG + 8;
+        if (segs < 2) segs = 2;
+        cap_cells = segs * SEG;
+        cells.reset(new Cell[cap_cells]);
+        nthreads = threads;
+        handles.reset(new Handle[threads]);
+        for (int i = 0; i < threads; ++i) {
+            Handle& h = handles[i];
+            h.next = &handles[(i + 1) % threads];
+            h.enq_peer = h.next;
+            h.deq_peer = h.next;
+        }
+    }
+    Cell* find_cell(u64 id) { return id < cap_cells ? &cells[id] : nullptr; }
+    static void advance_end(std::atomic<u64>& E, u64 cid) {
+        u64 e = E.load();
+        while (e < cid && !E.compare_exchange_strong(e, cid)) {}
+    }
+    static bool claim(std::atomic<u64>& st, u64 expect_id, u64 cell_id) {
+        u64 e = pst(1, expect_id);
+        return st.compare_exchange_strong(e, pst(0, cell_id));
+    }
+    void enq_commit(Cell* c, u64 v, u64 cid) {
+        advance_end(T, cid + 1);
+        c->val.exchange(v);
+    }
+    bool enq_fast(u64 v, u64* cid) {
+        u64 i = T.fetch_add(1);
+        Cell* c = find_cell(i);
+        if (!c) { *cid = i; return false; }
+        u64 e = BOTTOM;
+        if (c->val.compare_exchange_strong(e, v)) return true;
+        *cid = i;
+        return false;
+    }
+    bool enq_slow(Handle& h, u64 v, u64 cell_id) {
+        EnqReq& r = h.enq_req;
+        r.val.store(v);
+        r.state.store(pst(1, cell_id));
+        for (;;) {
+            u64 i = T.fetch_add(1);
+            Cell* c = find_cell(i);
+            if (!c) break;
+            u64 e = NUL;
+            if (c->enq.compare_exchange_strong(e, (u64)(uintptr_t)&r)) {
+                u64 cur = c->val.load();
+                if (cur == BOTTOM || cur == TOP) { claim(r.state, cell_id, i); break; }
+            }
+            if (!pend(r.state.load())) break;
+        }
+        u64 fid = low(r.state.load());
+        Cell* d = find_cell(fid);
+        if (d) {
+            if (d->val.load() == TOP) enq_commit(d, v, fid);
+            return true;
+        }
+        return false;
+    }
+    u64 help_enq(Handle& h, Cell* c, u64 i) {
+        u64 old = BOTTOM;
+        if (!c->val.compare_exchange_strong(old, TOP)) {
+            if (old != TOP) return old;
+        }
+        u64 ce = c->enq.load();
+        if (ce == NUL) {
+            Handle* p = h.enq_peer ? h.enq_peer : &h;
+            EnqReq* r = &p->enq_req;
+            u64 s = r->state.load();
+            u64 rid = low(s);
+            int pd = pend(s);
+            if (h.enq_id_last != 0 && h.enq_id_last != rid) {
+                h.enq_id_last = 0;
+                p = p->next;
+                h.enq_peer = p;
+                r = &p->enq_req;
+                s = r->state.load();
+                rid = low(s);
+                pd = pend(s);
+            }
+            if (pd && rid > 0 && rid <= i) {
+                u64 prev = NUL;
+                c->enq.compare_exchange_strong(prev, (u64)(uintptr_t)r);
+                if (prev != NUL && prev != (u64)(uintptr_t)r) {
+                    ce = prev;
+                    h.enq_id_last = rid;
+                } else {
+                    ce = (u64)(uintptr_t)r;
+                    h.enq_id_last = 0;
+                    h.enq_peer = p->next;
+                }
+            } else {
+                h.enq_id_last = 0;
+                h.enq_peer = p->next;
+            }
+            if (ce == NUL) {
+                u64 prev = NUL;
+                ce = c->enq.compare_exchange_strong(prev, TOPP) ? TOPP : prev;
+            }
+        }
+        if (ce == TOPP) return T.load() <= i ? EMPTY : RETRY;
+        EnqReq* r = (EnqReq*)(uintptr_t)ce;
+        u64 s = r->state.load();
+        int pd = pend(s);
+        u64 rid = low(s);
+        u64 v = r->val.load();
+        if (!pd) {
+            if (rid == i) {
+                if (c->val.load() == TOP) enq_commit(c, v, i);
+                return c->val.load();
+            }
+            return T.load() <= i ? EMPTY : RETRY;
+        }
+        if (rid > i) return T.load() <= i ? EMPTY : RETRY;
+        if (claim(r->state, rid, i) || r->state.load() == pst(0, i)) {
+            if (c->val.load() == TOP) enq_commit(c, v, i);
+        }
+        return c->val.load();
+    }
+    u64 deq_fast(Handle& h, u64* id) {
+        u64 i = H.fetch_add(1);
+        Cell* c = find_cell(i);
+        if (!c) { *id = i; return EMPTY; }
+        u64 v = help_enq(h, c, i);
+        if (v == EMPTY) return EMPTY;
+        if (v != TOP && v != RETRY) {
+            u64 e = NUL;
+            if (c->deq.compare_exchange_strong(e, TOPP)) return v;
+        }
+        *id = i;
+        return RETRY;
+    }
+    void help_deq(Handle& h, Handle& helpee) {
+        DeqReq& r = helpee.deq_req;
+        u64 s = r.state.load();
+        u64 id = r.id.load();
+        if (!pend(s) || low(s) < id) return;
+        u64 prior = id, i = id, cand = 0;
+        for (;;) {
+            s = r.state.load();
+            if (!pend(s) || r.id.load() != id) return;
+            while (!cand && pend(s) && low(s) == prior) {
+                Cell* c = find_cell(++i);
+                if (!c) break;
+                advance_end(H, i + 1);
+                u64 v = help_enq(h, c, i);
+                if (v == EMPTY || (v != TOP && v != RETRY && c->deq.load() == NUL)) { cand = i; break; }
+                s = r.state.load();
+                if (!pend(s) || r.id.load() != id) return;
+            }
+            if (cand) {
+                u64 e = pst(1, prior);
+                r.state.compare_exchange_strong(e, pst(1, cand));
+                cand = 0;
+            }
+            s = r.state.load();
+            if (!pend(s) || r.id.load() != id) return;
+            u64 a = low(s);
+            Cell* c = find_cell(a);
+            if (!c) return;
+            u64 cur = c->deq.load();
+            u64 e = NUL;
+            if (c->val.load() == TOP || c->deq.compare_exchange_strong(e, (u64)(uintptr_t)&r) ||
+                cur == (u64)(uintptr_t)&r) {
+                u64 se = s;
+                r.state.compare_exchange_strong(se, pst(0, a));
+                return;
+            }
+            prior = a;
+            if (a >= i) i = a;
+        }
+    }
+    u64 deq_slow(Handle& h, u64 cid) {
+        DeqReq& r = h.deq_req;
+        r.id.store(cid);
+        r.state.store(pst(1, cid));
+        help_deq(h, h);
+        u64 ix = low(r.state.load());
+        Cell* c = find_cell(ix);
+        if (!c) { advance_end(H, ix + 1); return EMPTY; }
+        u64 v = c->val.load();
+        advance_end(H, ix + 1);
+        return v == TOP ? EMPTY : v;
+    }
+    bool enqueue(u64 v, int tid) {
+        Handle& h = handles[tid];
+        for (int p = patience; p >= 0; --p) {
+            u64 cid = 0;
+            if (enq_fast(v, &cid)) return true;
+            if (p == 0) return enq_slow(h, v, cid);
+        }
+        return false;
+    }
+    u64 dequeue(int tid) {
+        Handle& h = handles[tid];
+        u64 v = RETRY, cid = 0;
+        for (int p = patience; p >= 0; --p) {
+            v = deq_fast(h, &cid);
+            if (v != RETRY) break;
+        }
+        if (v == RETRY) v = deq_slow(h, cid);
+        if (v != EMPTY) {
+            help_deq(h, *h.deq_peer);
+            h.deq_peer = h.deq_peer->next;
+        }
+        return v;
+    }
+};
+
+}  // namespace ymc
+
+// =============================================================================
+// Uniform front end
+// =============================================================================
+
+struct AnyQueue {
+    int kind = 0;
+    gwf::Mpmc* g = nullptr;
+    glf::Mpmc* l = nullptr;
+    ymc::Queue* y = nullptr;
+    sfq::Queue* s = nullptr;
+    ~AnyQueue() { delete g; delete l; delete y; delete s; }
+};
+
+static int bits_for(u32 max_threads) {
+    int b = 5;
+    while (((1ULL << b) - 1) < (u64)max_threads + 1) ++b;   // NULL_TID must stay free
+    return b;
+}
+
+static AnyQueue* make_queue(int kind, u32 order, u32 threads, int ops_hint) {
+    AnyQueue* q = new AnyQueue;
+    q->kind = kind;
+    u32 n = 1u << order;
+    switch (kind) {
+        case GWFQ: {
+            q->g = new gwf::Mpmc;
+            q->g->init(n, std::max<u32>(threads, 32), bits_for(std::max<u32>(threads, 32)), gwf::Knobs{});
+            break;
+        }
+        case GLFQ: q->l = new glf::Mpmc; q->l->init(n); break;
+        case WFQ: q->y = new ymc::Queue; q->y->init((int)threads, ops_hint); break;
+        case SFQ: q->s = new sfq::Queue; q->s->init(n); break;
+        default: delete q; return nullptr;
+    }
+    return q;
+}
+
+// The harness shims of throughout_bench.cpp:134-285 / history.cpp:56-140.
+static inline bool q_enqueue(AnyQueue* q, u64 v, u32 tid, bool split) {
+    switch (q->kind) {
+        case GWFQ: return q->g->enqueue(v, tid);
+        case GLFQ: return q->l->enqueue(v);
+        case WFQ: return q->y->enqueue(v, (int)tid);
+        default: {
+            u32 x = (u32)(v ^ (v >> 32));       // throughout_bench.cpp:246-249
+            if (x == 0) x = 1;
+            return (split ? q->s->enqueue_nb(x) : q->s->enqueue_blocking(x)) == sfq::SUCCESS;
+        }
+    }
+}
+static inline bool q_dequeue(AnyQueue* q, u64* out, u32 tid, bool split) {
+    switch (q->kind) {
+        case GWFQ: return q->g->dequeue(out, tid);
+        case GLFQ: return q->l->dequeue(out);
+        case WFQ: { u64 v = q->y->dequeue((int)tid); if (v == ymc::EMPTY) return false; *out = v; return true; }
+        default: {
+            u32 item = 0;
+            int rc = split ? q->s->dequeue_nb(&item) : q->s->dequeue_blocking(&item);
+            if (rc != sfq::SUCCESS) return false;
+            *out = item;
+            return true;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+typedef struct {
+    uint64_t proc;
+    uint32_t op;
+    uint32_t _pad;
+    uint64_t arg;
+    uint64_t ret;
+    int64_t call;
+    int64_t end;
+} oracle_hist_rec;
+
+typedef struct {
+    uint64_t enq_success, enq_fail, deq_success, deq_empty;
+    double elapsed_ms;
+    uint32_t threads;
+    uint32_t _pad;
+} oracle_tb_stats;
+
+// History of `threads` host threads each doing `ops` operations (mode 0:
+// enqueue then dequeue; mode 1: the first producer_percent% of threads only
+// enqueue, the rest only dequeue), bracketed by a shared logical clock.
+// value_mode 0: (tid<<32)|(seq+1) (history.cpp:184); 1: 32-bit (tid<<16)|(seq+1).
+// SFQ uses the non-blocking operations and the 15+16-bit encoding of
+// history.cpp:121-140 whatever value_mode says; its BUSY dequeues are written as
+// op 2 (dequeue without effect).  Returns records written.
+int64_t oracle_history(int kind, uint32_t order, uint32_t threads, uint32_t ops, int mode,
+                       int producer_percent, int value_mode, oracle_hist_rec* out, uint64_t cap) {
+    uint64_t need = (uint64_t)threads * ops * (mode == 0 ? 2 : 1);
+    if (need > cap) return -1;
+    std::unique_ptr<AnyQueue> q(make_queue(kind, order, threads, (int)ops * 2 + 8));
+    if (!q) return -2;
+    std::atomic<uint64_t> clock{1};
+    std::atomic<int> ready{0};
+    std::vector<std::thread> ths;
+    std::vector<uint64_t> counts(threads, 0);
+    const uint64_t stride = (uint64_t)ops * (mode == 0 ? 2 : 1);
+    for (uint32_t t = 0; t < threads; ++t) {
+        ths.emplace_back([&, t]() {
+            ready.fetch_add(1);
+            while (ready.load() < (int)threads) cpu_relax();
+            oracle_hist_rec* rec = out + (uint64_t)t * stride;
+            uint64_t k = 0;
+            bool producer = ((uint64_t)t * 100 / threads) < (uint64_t)producer_percent;
+            for (uint32_t i = 0; i < ops; ++i) {
+                u64 v;
+                if (kind == SFQ) v = (((u64)t & 0x7FFF) << 16) | ((i + 1) & 0xFFFF);
+                else if (value_mode == 1) v = (((u64)t & 0xFFFF) << 16) | ((i + 1) & 0xFFFF);
+                else v = ((u64)t << 32) | (u64)(i + 1);
+                if (mode == 0 || producer) {
+                    oracle_hist_rec& r = rec[k++];
+                    r.proc = t; r.op = 0; r._pad = 0; r.arg = v;
+                    r.call = (int64_t)clock.fetch_add(1);
+                    bool ok = q_enqueue(q.get(), v, t, true);
+                    r.ret = ok ? 1 : 0;
+                    r.end = (int64_t)clock.fetch_add(1);
+                }
+                if (mode == 0 || !producer) {
+                    oracle_hist_rec& r = rec[k++];
+                    r.proc = t; r.op = 1; r._pad = 0; r.arg = 0;
+                    r.call = (int64_t)clock.fetch_add(1);
+                    u64 o = 0;
+                    bool ok = q_dequeue(q.get(), &o, t, true);
+                    r.ret = ok ? o : 0;
+                    r.end = (int64_t)clock.fetch_add(1);
+                    // SFQ's non-blocking dequeue fails with BUSY, not "empty": record the
+                    // no-op dequeue (op 2) that the checker models for it.
+                    if (!ok && kind == SFQ) r.op = 2;
+                }
+            }
+            counts[t] = k;
+        });
+    }
+    for (auto& th : ths) th.join();
+    // compact per-thread blocks (split mode writes `ops` records per thread)
+    uint64_t n = 0;
+    for (uint32_t t = 0; t < threads; ++t) {
+        oracle_hist_rec* rec = out + (uint64_t)t * stride;
+        for (uint64_t i = 0; i < counts[t]; ++i) out[n++] = rec[i];
+    }
+    return (int64_t)n;
+}
+
+// Fixed-duration throughput run (throughout_bench.cpp:959-1051) with host threads.
+// mode 0 balanced (enqueue then dequeue per iteration), 1 split.
+int oracle_tb_run(int kind, uint32_t order, uint32_t threads, int mode, int producer_percent,
+                  double warmup_ms, double run_ms, oracle_tb_stats* out) {
+    std::unique_ptr<AnyQueue> q(make_queue(kind, order, threads, 512));
+    if (!q) return -2;
+    std::atomic<int> phase{0};   // 0 warmup, 1 timed, 2 stop
+    std::atomic<int> ready{0};
+    struct alignas(128) Ctr { uint64_t eo = 0, ef = 0, dok = 0, de = 0; };
+    std::vector<Ctr> ctr(threads);
+    std::vector<std::thread> ths;
+    for (uint32_t t = 0; t < threads; ++t) {
+        ths.emplace_back([&, t]() {
+            ready.fetch_add(1);
+            bool producer = ((uint64_t)t * 100 / threads) < (uint64_t)producer_percent;
+            Ctr local;
+            uint32_t i = 0;
+            bool counting = false;
+            for (;;) {
+                int ph = phase.load(std::memory_order_relaxed);
+                if (ph == 2) break;
+                if (ph == 1 && !counting) { counting = true; local = Ctr{}; }
+                for (int c = 0; c < 64; ++c, ++i) {
+                    if (mode == 0) {
+                        u64 v = ((u64)t << 32) ^ (u64)(i + 1) ^ 0x9e3779b97f4a7c15ULL;
+                        if (q_enqueue(q.get(), v, t, false)) local.eo++; else local.ef++;
+                        u64 o;
+                        if (q_dequeue(q.get(), &o, t, false)) local.dok++; else local.de++;
+                    } else if (producer) {
+                        u64 v = ((u64)t << 32) ^ (u64)(i + 1) ^ 0x517cc1b727220a95ULL;
+                        if (q_enqueue(q.get(), v, t, true)) local.eo++; else local.ef++;
+                    } else {
+                        u64 o;
+                        if (q_dequeue(q.get(), &o, t, true)) local.dok++; else local.de++;
+                    }
+                }
+            }
+            ctr[t] = local;
+        });
+    }
+    while (ready.load() < (int)threads) std::this_thread::yield();
+    std::this_thread::sleep_for(std::chrono::duration<double, std::milli>(warmup_ms));
+    auto t0 = clk::now();
+    phase.store(1);
+    std::this_thread::sleep_for(std::chrono::duration<double, std::milli>(run_ms));
+    phase.store(2);
+    auto t1 = clk::now();
+    for (auto& th : ths) th.join();
+    std::memset(out, 0, sizeof(*out));
+    for (auto& c : ctr) {
+        out->enq_success += c.eo; out->enq_fail += c.ef;
+        out->deq_success += c.dok; out->deq_empty += c.de;
+    }
+    // Operations finish their current 64-op batch after the stop flag; count the
+    // elapsed time to the last join so that the rate is not overstated.
+    auto t2 = clk::now();
+    (void)t1;
+    out->elapsed_ms = std::chrono::duration<double, std::milli>(t2 - t0).count();
+    out->threads = threads;
+    return 0;
+}
+
+// Produce-then-drain FIFO check (throughout_bench.cpp:531-603) on host threads.
+// Exactly-once is checked as in the reference (counts per token).  The reference's
+// per-producer order check (an atomicMax over last_seq, :585-588) starts from
+// 0xFFFFFFFF (:691) and so never fires; here every dequeue is bracketed by a shared
+// logical clock instead, and an order error is a pair of tokens from one producer,
+// seq a < seq b, whose dequeue of b returned before the dequeue of a was called.
+// out_counts = [in, out, dup, order_err, missing+oob].  Returns 0 when clean.
+int oracle_fifo_check(int kind, uint32_t order, uint32_t threads, uint32_t ops_per_thread,
+                      uint64_t* out_counts) {
+    std::unique_ptr<AnyQueue> q(make_queue(kind, order, threads, (int)ops_per_thread * 2 + 8));
+    if (!q) return -2;
+    std::vector<std::thread> ths;
+    for (uint32_t t = 0; t < threads; ++t)
+        ths.emplace_back([&, t]() {
+            for (uint32_t i = 0; i < ops_per_thread; ++i) {
+                u64 tok = kind == SFQ ? ((((u64)t & 0x7FFF) << 16) | ((i + 1) & 0xFFFF))
+                                      : (((u64)t << 32) | (u64)(i + 1));
+                auto t0 = clk::now();
+                while (!q_enqueue(q.get(), tok, t, true)) {
+                    cpu_relax();
+                    if (std::chrono::duration<double>(clk::now() - t0).count() > 10.0) return;
+                }
+            }
+        });
+    for (auto& th : ths) th.join();
+    ths.clear();
+    const uint64_t total = (uint64_t)threads * ops_per_thread;
+    std::vector<std::atomic<uint32_t>> cnt(total);
+    std::vector<int64_t> call(total, 0), end(total, 0);
+    for (auto& c : cnt) c.store(0);
+    std::atomic<uint64_t> consumed{0}, dup{0}, oob{0}, clock{1};
+    for (uint32_t t = 0; t < threads; ++t)
+        ths.emplace_back([&, t]() {
+            auto t0 = clk::now();
+            while (consumed.load() < total) {
+                u64 v = 0;
+                int64_t c0 = (int64_t)clock.fetch_add(1);
+                bool ok = q_dequeue(q.get(), &v, t, true);
+                int64_t c1 = (int64_t)clock.fetch_add(1);
+                if (!ok) {
+                    cpu_relax();
+                    if (std::chrono::duration<double>(clk::now() - t0).count() > 10.0) return;
+                    continue;
+                }
+                if (consumed.fetch_add(1) >= total) continue;
+                u32 ptid, seq;
+                if (kind == SFQ) { ptid = (u32)(v >> 16) & 0x7FFF; seq = (u32)(v & 0xFFFF) - 1; }
+                else { ptid = (u32)(v >> 32); seq = (u32)v - 1; }
+                if (ptid >= threads || seq >= ops_per_thread) { oob++; continue; }
+                u64 slot = (u64)ptid * ops_per_thread + seq;
+                if (cnt[slot].fetch_add(1) >= 1) { dup++; continue; }
+                call[slot] = c0;
+                end[slot] = c1;
+            }
+        });
+    for (auto& th : ths) th.join();
+    uint64_t missing = 0, ord = 0;
+    for (uint32_t p = 0; p < threads; ++p) {
+        int64_t max_call = -1;
+        for (uint32_t s = 0; s < ops_per_thread; ++s) {
+            u64 slot = (u64)p * ops_per_thread + s;
+            if (cnt[slot].load() == 0) { missing++; continue; }
+            if (end[slot] < max_call) ord++;
+            max_call = std::max(max_call, call[slot]);
+        }
+    }
+    if (out_counts) {
+        out_counts[0] = total; out_counts[1] = std::min<uint64_t>(consumed.load(), total);
+        out_counts[2] = dup.load(); out_counts[3] = ord; out_counts[4] = missing + oob.load();
+    }
+    return (consumed.load() >= total && !dup && !missing && !oob && !ord) ? 0 : 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,41 @@
+"""The std::atomic CPU restatements of the four queues (oracle/cpu_queues.cpp):
+their histories must check linearizable and their FIFO drains must be exact.
+These are the CPU baseline and reference arm, so they are pinned here."""
+import pytest
+
+KINDS = ["gwfq", "glfq", "wfq", "sfq"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("threads,ops", [(8, 16), (32, 16), (64, 16)])
+def test_cpu_history_linearizable(oracle_lib, kind, threads, ops):
+    h = oracle_lib.cpu_history(kind, threads, ops)
+    assert len(h) == threads * ops * 2
+    assert oracle_lib.check(h) == "Linearizable (FIFO)"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_cpu_split_history_linearizable(oracle_lib, kind):
+    h = oracle_lib.cpu_history(kind, 16, 32, mode=1, producer_percent=50)
+    assert oracle_lib.check(h) == "Linearizable (FIFO)"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_cpu_fifo_drain(oracle_lib, kind):
+    r = oracle_lib.cpu_fifo_check(kind, 8, 64)
+    assert r["verified"], r
+    assert r["in"] == r["out"] == 8 * 64
+
+
+@pytest.mark.parametrize("kind", ["gwfq", "glfq"])
+def test_cpu_small_ring_wraps(oracle_lib, kind):
+    # capacity 2^4 with 8 threads: the rings wrap many cycles during the history
+    h = oracle_lib.cpu_history(kind, 8, 64, order=4)
+    assert oracle_lib.check(h) == "Linearizable (FIFO)"
+
+
+def test_cpu_throughput_counts(oracle_lib):
+    r = oracle_lib.cpu_throughput("gwfq", 4, mode=0, run_ms=50, warmup_ms=10)
+    # balanced: every thread enqueues then dequeues; at most `threads` values stay queued
+    assert r["enq_success"] > 0
+    assert r["enq_success"] - r["deq_success"] <= 4 + 64 * 4
