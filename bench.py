@@ -1,0 +1,311 @@
+"""Queue throughput benchmark (the reference's throughput harness, balanced mode).
+
+Workload: G-WFQ, balanced mode (every thread enqueues then dequeues,
+throughout_bench.cpp:810-840), capacity 2^20, 262144 threads in blocks of 256,
+128 operations per thread per chunk, uint32 payloads from a seed.  A step is one
+chunk launch over all threads.  Metric: successful queue operations per second
+(enq_success + deq_success, throughout_bench.cpp:894), in Mops/s.
+
+  value    device time of K chunk launches (CUDA events on the launching stream),
+           L2 flushed between steps by writing a 256 MiB buffer
+  e2e      the same chunks through the C-ABI entry point gcq_tb_chunk_host with the
+           payloads in pinned host memory: host->device copy, kernel, and the
+           counters read back to the host are inside the timed region
+  roofline the chunk kernel against the measured L2 atomic throughput of this GPU
+           (gcq_roofline_measure, run in the same process)
+  cpu_baseline the oracle's std::atomic G-WFQ on all host cores (a reported
+           baseline, not the target)
+
+--impl reference runs the reference algorithm on the host cores instead: the
+reference is HIP for AMD GPUs and cannot run here, so its arm is the oracle's CPU
+restatement of the same G-WFQ (oracle/cpu_queues.cpp), on every host core.
+
+Multi-GPU (torchrun, --gpus N): replicas only -- a queue is one linearizable object
+with global counters, so each rank runs its own queue; value = all ranks' operations
+over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+KIND = "gwfq"
+CAPACITY_LOG2 = 20
+THREADS = 262144
+BLOCK = 256
+CHUNK_OPS = 128
+# algorithmic L2 atomics per successful operation: each user operation is two ring
+# operations (indirection through fq/aq), each one entry RMW (CAS or OR) plus a
+# 1/32 share of a warp-aggregated ticket fetch-and-add
+ATOMICS_PER_OP = 2.0 + 2.0 / 32.0
+METRIC = "queue succ Mops/s (G-WFQ balanced)"
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(seconds=3.0, order=CAPACITY_LOG2):
+    """The oracle's G-WFQ (std::atomic, the reference algorithm) on all host cores."""
+    from oracle import lib as olib
+    cores = os.cpu_count() or 1
+    r = olib.cpu_throughput("gwfq", cores, mode=0, order=order, warmup_ms=200, run_ms=seconds * 1000)
+    return {"value": round(r["succ_mops"], 3), "unit": "Mops/s", "cores": cores, "kind": "port",
+            "sample": "balanced G-WFQ (oracle/cpu_queues.cpp), %d host threads, capacity 2^%d, %.1f s timed"
+                      % (cores, order, seconds)}
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    from oracle import build as obuild, lib as olib
+    obuild.build()
+    cores = os.cpu_count() or 1
+    step_ms = 400.0
+    for _ in range(args.warmup):
+        olib.cpu_throughput("gwfq", cores, mode=0, order=CAPACITY_LOG2, warmup_ms=50, run_ms=step_ms)
+    ops = 0
+    ms = 0.0
+    for _ in range(args.steps):
+        r = olib.cpu_throughput("gwfq", cores, mode=0, order=CAPACITY_LOG2, warmup_ms=50, run_ms=step_ms)
+        ops += r["enq_success"] + r["deq_success"]
+        ms += r["elapsed_ms"]
+    value = ops / (ms * 1e3)
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mops/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "gwfq balanced, capacity 2^20, %d host threads (reference algorithm on "
+                                   "the host cores; the HIP reference has no NVIDIA/CPU build)" % cores,
+                       "threads": cores, "capacity_log2": CAPACITY_LOG2},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mops/s", "cores": cores, "kind": "port",
+                             "sample": "%d steps of %.0f ms, balanced G-WFQ, %d host threads"
+                                       % (args.steps, step_ms, cores)},
+            "e2e": {"value": round(value, 3), "unit": "Mops/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import gcq_gb300 as g
+
+    rank, world, local = _env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    threads, chunk = args.threads, args.chunk_ops
+    q = g.Queue(KIND, args.capacity_log2, threads)
+    ctr = torch.zeros(4, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    peaks = g.roofline(reps=3) if rank == 0 else None
+
+    def step(seed):
+        q.tb_launch(0, threads, chunk, ctr.data_ptr(), block=BLOCK, seed=seed, stream=sptr)
+
+    for w in range(args.warmup):
+        step(1000 + w)
+        flush.zero_()
+    torch.cuda.synchronize()
+    ctr.zero_()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        step(i)
+        ev[i][1].record(stream)
+        flush.zero_()          # outside the event pair: evicts L2 between steps
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = sum(step_ms)
+    c = ctr.cpu().tolist()
+    succ = c[0] + c[2]
+    err = q.error_word()
+    if err & ~g.ERR_POOL:
+        raise RuntimeError("queue error word 0x%x during the bench" % err)
+    # whole-job: every rank's operations over the slowest rank's time
+    if world > 1:
+        t = torch.tensor([dev_ms, float(succ)], dtype=torch.float64, device=dev)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        dev_ms_all, succ_all = mx[0].item(), t[1].item()
+    else:
+        dev_ms_all, succ_all = dev_ms, float(succ)
+    value = succ_all / (dev_ms_all * 1e3)
+
+    # ---- end to end through the C ABI with host buffers -----------------------
+    rng = np.random.default_rng(12345)
+    pin = torch.empty(threads * chunk, dtype=torch.int32).pin_memory()
+    pay = pin.numpy().view(np.uint32)
+    pay[:] = rng.integers(0, 2**32, size=threads * chunk, dtype=np.uint64).astype(np.uint32)
+    for w in range(max(1, args.warmup)):
+        q.tb_chunk_host(0, threads, chunk, pay, block=BLOCK, stream=sptr)
+    torch.cuda.synchronize()
+    e2e_ops, e2e_s = 0, 0.0
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cc = q.tb_chunk_host(0, threads, chunk, pay, block=BLOCK, stream=sptr)
+        e2e_s += time.perf_counter() - t0
+        e2e_ops += cc["enq_success"] + cc["deq_success"]
+    if world > 1:
+        t = torch.tensor([e2e_s, float(e2e_ops)], dtype=torch.float64, device=dev)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        e2e_s, e2e_ops = mx[0].item(), t[1].item()
+    e2e = e2e_ops / (e2e_s * 1e6)
+
+    if rank == 0:
+        per_launch_ms = dev_ms / args.steps
+        atom_rate = succ / args.steps * ATOMICS_PER_OP / (per_launch_ms * 1e-3)
+        peak_rs = max(peaks["rs_lines"], peaks["rs_contig"])
+        roof = {
+            "bound": "l2_atomic",
+            "achieved": round(atom_rate / 1e9, 3),
+            "peak": round(peak_rs / 1e9, 3),
+            "unit": "Gatomic/s",
+            "frac": round(atom_rate / peak_rs, 4),
+            "traffic": None,
+            "kernel": "k_tb_chunk<GCQ_GWFQ>",
+            "peak_source": "measured in this run by gcq_roofline_measure: max of spread 64-bit "
+                           "fetch-add on distinct lines (%.1f G/s) and warp-contiguous words (%.1f G/s)"
+                           % (peaks["rs_lines"] / 1e9, peaks["rs_contig"] / 1e9),
+            "ticket_ceiling_mops": round(peaks["r1_warp"] / 4 / 1e6, 1),
+            "single_address_gatomic_s": round(peaks["r1_single"] / 1e9, 3),
+            "hbm_measured_gbs": round(peaks["hbm_gbs"], 1),
+        }
+        mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(mp):
+            roof["hbm_peak_gbs_of_measured"] = json.load(open(mp)).get("hbm_gbs")
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mops/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms_all / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (uint32 payloads from a seed)",
+            "config": {"workload": "gwfq balanced, capacity 2^%d, %d threads, block %d, %d ops/thread/chunk"
+                                   % (args.capacity_log2, threads, BLOCK, chunk),
+                       "queue": KIND, "mode": "balanced", "capacity_log2": args.capacity_log2,
+                       "threads": threads, "block": BLOCK, "chunk_ops": chunk,
+                       "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "1 gpu"},
+            "e2e": {"value": round(e2e, 3), "unit": "Mops/s",
+                    "h2d_bytes_per_step": threads * chunk * 4, "d2h_bytes_per_step": 32},
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+            "roofline": roof,
+            "step_ms": {"min": round(min(step_ms), 4), "median": round(statistics.median(step_ms), 4),
+                        "max": round(max(step_ms), 4)},
+            "counters": {"enq_success": c[0], "enq_fail": c[1], "deq_success": c[2], "deq_empty": c[3]},
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    q.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gcq", "reference"], default="gcq")
+    ap.add_argument("--threads", type=int, default=THREADS)
+    ap.add_argument("--chunk-ops", type=int, default=CHUNK_OPS)
+    ap.add_argument("--capacity-log2", type=int, default=CAPACITY_LOG2)
+    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -50,6 +50,12 @@ class FifoResult(C.Structure):
                 ("_pad", C.c_int)]
 
 
+class Roofline(C.Structure):
+    _fields_ = [("r1_single", C.c_double), ("r1_warp", C.c_double), ("rs_lines", C.c_double),
+                ("rs_contig", C.c_double), ("rc_lines", C.c_double), ("rc128_lines", C.c_double),
+                ("hbm_gbs", C.c_double), ("sms", C.c_int), ("_pad", C.c_int)]
+
+
 class GcqError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = status
@@ -78,6 +84,7 @@ SIGNATURES = {
     "gcq_tb_chunk_host": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
     "gcq_tb_run": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
     "gcq_fifo_check": ([P, U32, U32, U32, C.POINTER(FifoResult)], I32),
+    "gcq_roofline_measure": ([C.POINTER(Roofline), I32], I32),
 }
 
 _LIB = None
@@ -216,6 +223,13 @@ class Queue:
         r = FifoResult()
         _check(_lib().gcq_fifo_check(self._h, threads, block, ops_per_thread, C.byref(r)), "gcq_fifo_check")
         return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+
+def roofline(reps: int = 3) -> dict:
+    """Measure the atomic roofline of the current GPU (gcq_roofline_measure)."""
+    r = Roofline()
+    _check(_lib().gcq_roofline_measure(C.byref(r), reps), "gcq_roofline_measure")
+    return {f: getattr(r, f) for f, _ in Roofline._fields_ if not f.startswith("_")}
 
 
 def history_to_jsonl(recs: np.ndarray, path: str, reference_format: bool = False):

@@ -193,13 +193,15 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
             const uint64_t o_ah = take((uint64_t)max_threads * sizeof(gcq::gwf::helper_state));
             const uint64_t o_fh = take((uint64_t)max_threads * sizeof(gcq::gwf::helper_state));
             const uint64_t o_d = take(n * 8);
+            const uint64_t o_ao = take(2 * n * 4), o_fo = take(2 * n * 4);
             q->bytes = align_up(off, A);
             if (cudaMalloc(&q->base, q->bytes) != cudaSuccess) { delete q; return GCQ_ENOMEM; }
             char* b = (char*)q->base;
             gcq::gwf::mpmc h;
             memset(&h, 0, sizeof h);
-            auto fill = [&](gcq::gwf::ring& r, uint64_t oe, uint64_t orr, uint64_t oh) {
+            auto fill = [&](gcq::gwf::ring& r, uint64_t oe, uint64_t orr, uint64_t oh, uint64_t oo) {
                 r.Entry = (gcq::u64a*)(b + oe);
+                r.Owner = (gcq::u32a*)(b + oo);
                 r.Record = (gcq::gwf::record*)(b + orr);
                 r.Help = (gcq::gwf::helper_state*)(b + oh);
                 r.err = (gcq::u32a*)(b + o_err);
@@ -211,8 +213,8 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
                 r.deq_patience = k.deq_patience;
                 r.remap = k.remap ? 1u : 0u;
             };
-            fill(h.aq, o_ae, o_ar, o_ah);
-            fill(h.fq, o_fe, o_fr, o_fh);
+            fill(h.aq, o_ae, o_ar, o_ah, o_ao);
+            fill(h.fq, o_fe, o_fr, o_fh, o_fo);
             h.data = (gcq::u64a*)(b + o_d);
             h.err = (gcq::u32a*)(b + o_err);
             q->obj = b + o_hdr;

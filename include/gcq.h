@@ -180,6 +180,25 @@ typedef struct gcq_fifo_result {
 int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
                    gcq_fifo_result* out);
 
+/* ------------------------------------------------------------- roofline ----
+ * The atomic roofline of this GPU, measured by a microbenchmark in the same
+ * process (the reference reports raw Mops/s only).  Rates are operations per
+ * second (r1_warp: tickets per second); hbm_gbs is copy read+write GB/s. */
+typedef struct gcq_roofline {
+    double r1_single;    /* one 64-bit word, atomicAdd from every thread */
+    double r1_warp;      /* one word, warp-aggregated tickets */
+    double rs_lines;     /* spread fetch-add, one 128-B line per thread */
+    double rs_contig;    /* spread fetch-add, a warp on 32 consecutive words */
+    double rc_lines;     /* spread 64-bit CAS, one line per thread */
+    double rc128_lines;  /* spread 128-bit CAS (atom.cas.b128) */
+    double hbm_gbs;      /* device copy bandwidth */
+    int sms;
+    int _pad;
+} gcq_roofline;
+
+/* Run the microbenchmark (best of `reps`); synchronises the device. */
+int gcq_roofline_measure(gcq_roofline* out, int reps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,7 +17,11 @@
 //   * Tail, Head and Threshold each own a 128-byte line;
 //   * the private help countdown (nextCheck/nextTid) lives in a dense per-thread
 //     array apart from the shared record, so a warp reads it in one coalesced access
-//     and helpers never share its line.
+//     and helpers never share its line;
+//   * a per-slot owner table names the record of the slow-path enqueuer that
+//     produced an Enq=0 entry, so finalize_request goes to that record directly
+//     instead of scanning all max_threads records (gwf_ring.hpp:316-327), which at
+//     2^18 threads costs 2^18 dependent loads per consume.
 #pragma once
 
 #include <stdint.h>
@@ -108,12 +112,13 @@ struct alignas(128) ring {
     record* Record;         // max_threads shared records
     helper_state* Help;     // max_threads private countdowns
     u32a* err;              // sticky error word
+    u32a* Owner;            // 2N: 1 + index of the record whose slow-path enqueue last
+                            // produced an Enq=0 entry in the slot (0 = none)
     uint32_t order;         // log2 N
     uint32_t thr_bits;      // width of the ThrIdx field
     uint32_t max_threads;   // number of records; thread indices must be below it
     uint32_t help_delay, enq_patience, deq_patience;
     uint32_t remap;         // 1: spread consecutive tickets over different lines
-    uint32_t _pad3;
 };
 
 // Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345).
@@ -130,6 +135,7 @@ struct cfg {
     record* rec;
     helper_state* help;
     u32a* err;
+    u32a* owner;
     uint32_t order, thr_bits, max_threads;
     uint32_t help_delay, enq_patience, deq_patience, remap;
     __host__ __device__ __forceinline__ uint32_t slots() const { return 2u << order; }
@@ -159,7 +165,7 @@ struct cfg {
 
 __device__ __forceinline__ cfg load_cfg(const ring* q) {
     cfg c;
-    c.entry = q->Entry; c.rec = q->Record; c.help = q->Help; c.err = q->err;
+    c.entry = q->Entry; c.rec = q->Record; c.help = q->Help; c.err = q->err; c.owner = q->Owner;
     c.order = q->order; c.thr_bits = q->thr_bits; c.max_threads = q->max_threads;
     c.help_delay = q->help_delay; c.enq_patience = q->enq_patience; c.deq_patience = q->deq_patience;
     c.remap = q->remap;
@@ -217,6 +223,7 @@ struct wf_t {
     unsigned long long Entry[SLOTS];
     gcq::gwf::record Record[Config::MAX_THREADS];
     gcq::gwf::helper_state Help[Config::MAX_THREADS];
+    gcq::u32a Owner[SLOTS];
 };
 
 template <typename Config, uint32_t N_PARAM>

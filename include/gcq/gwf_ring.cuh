@@ -32,6 +32,7 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
         c.entry[s] = (full && pos < n)
                          ? entry::pack(0xFF, c.cycle_of((uint64_t)slots + pos), true, true, pos)
                          : entry::INIT;
+        c.owner[s] = 0;
     }
     for (uint64_t i = gid; i < c.max_threads; i += nthreads) {
         record* r = &c.rec[i];
@@ -52,9 +53,18 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
 
 // ------------------------------------------------------------------ consume etc.
 // finalize_request, gwf_ring.hpp:309-328: set FIN on the slow-path enqueuer whose
-// localTail holds ticket h.
-__device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t tid) {
+// localTail holds ticket h.  The slot's owner entry names that record; the scan of
+// all records remains as the fallback when it no longer matches.
+__device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j, uint32_t tid) {
     const uint64_t h_local = h_raw << 2;
+    const uint32_t own = ld_rlx(&c.owner[j]);
+    if (own != 0 && own <= c.max_threads) {
+        const uint64_t lt = ld_acq(&c.rec[own - 1].localTail);
+        if ((lt & local::CNT_MASK) == h_local) {
+            cas(&c.rec[own - 1].localTail, h_local, h_local | local::FIN);
+            return;
+        }
+    }
     uint32_t i = (tid + 1 == c.max_threads) ? 0 : tid + 1;
     while (i != tid) {
         const uint64_t lt = ld_acq(&c.rec[i].localTail);
@@ -68,7 +78,7 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t t
 
 // consume, gwf_ring.hpp:335-341
 __device__ __forceinline__ void consume(const cfg& c, uint64_t h_raw, uint32_t j, uint64_t e, uint32_t tid) {
-    if (!entry::enq(e)) finalize_request(c, h_raw, tid);
+    if (!entry::enq(e)) finalize_request(c, h_raw, j, tid);
     fetch_or(&c.entry[j], entry::CONSUME_MASK);
 }
 
@@ -237,7 +247,9 @@ __device__ inline bool try_enq_slow(ring* q, const cfg& c, uint64_t T_raw, uint3
                 if (!cas_upd(&c.entry[j], &P, nn)) continue;
                 return false;
             }
-            // two-step insertion: Enq=0 first, flipped to 1 once FIN is set
+            // two-step insertion: Enq=0 first, flipped to 1 once FIN is set; the
+            // owner entry is published by the release half of the CAS below
+            st_rlx(&c.owner[j], (uint32_t)(r - c.rec) + 1u);
             const uint64_t nn = entry::pack(enote, tcyc, true, false, index);
             if (!cas_upd(&c.entry[j], &P, nn)) continue;
             const uint64_t T_local = T_raw << 2;
@@ -428,6 +440,7 @@ __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
     h->Entry = q->Entry;
     h->Record = q->Record;
     h->Help = q->Help;
+    h->Owner = q->Owner;
     q->err = 0;
     h->err = &q->err;
     h->order = 31 - __clz(N_PARAM);
@@ -445,7 +458,7 @@ __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
     // single thread: the slice covers the whole ring (no block sync needed
     // because gid 0 of a 1-thread group owns every element)
     const gcq::gwf::cfg c = gcq::gwf::load_cfg(h);
-    for (uint32_t i = 0; i < c.slots(); ++i) c.entry[i] = gcq::gwf::entry::INIT;
+    for (uint32_t i = 0; i < c.slots(); ++i) { c.entry[i] = gcq::gwf::entry::INIT; c.owner[i] = 0; }
     if (full)
         for (uint32_t i = 0; i < N_PARAM; ++i) {
             const uint64_t t = (uint64_t)c.slots() + i;

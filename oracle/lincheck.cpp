@@ -167,67 +167,127 @@ public:
     // Pruning beyond the published method: only enqueues are branch points.
     //  * An operation that is legal now and leaves the state unchanged (failed
     //    enqueue, failed-without-effect dequeue, "empty" on an empty queue) is
-    //    linearised at once and never skipped: the state is the same either way and
-    //    taking it only relaxes the real-time constraint of its return event.
+    //    linearised at once: the state is the same either way and taking it only
+    //    relaxes the real-time constraint of its return event.
     //  * A dequeue whose value is at the head is also taken at once: in any
     //    successful order from here, everything before it is an enqueue or a no-op
     //    (no other dequeue can return the head, no "empty" can see a non-empty
     //    queue), so moving it first stays legal, and its call is already due.
-    // So when every continuation after such a step fails, skipping it would fail too,
-    // and the search backtracks past it instead of trying the next candidate.
+    // At every node these dominant operations are taken first, before any enqueue is
+    // tried; when every continuation after one fails, skipping it would fail too, so
+    // the search backtracks past it to the last enqueue choice.  With distinct values
+    // the operation whose return is next decides what can help: if it is a dequeue
+    // that is not dominant, only its own value's enqueue into an empty queue can
+    // (anything else, including more enqueues, only delays the failure).
     int run(double timeout_s) {
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<uint64_t> bits(words_, 0);
         uint64_t bits_hash = 0;
         std::deque<uint64_t> state;
-        struct Frame { Event* call; int kind; uint64_t val; };
+        struct Frame { Event* call; int kind; uint64_t val; int cand; };
         std::vector<Frame> stack;
-        Event* e = head_.next;
         uint64_t iters = 0;
-        bool backtrack = false;
+        bool backtrack = false, fresh = true;
+        int next_cand = 0;          // first enqueue candidate to try at this node
+        std::vector<Event*> cands;
+        // apply op of call event x; false if illegal; on success pushes a frame or,
+        // when the configuration was seen before, undoes it and requests a backtrack
+        auto take = [&](Event* x, int* kind_out) -> int {
+            const Op& o = ops_[x->op];
+            int kind = 0;
+            const uint64_t popped = state.empty() ? 0 : state.front();
+            if (o.is_enq && o.ok && !o.noop && !order_ok(x->op)) return 0;
+            if (!model_step(state, o, &kind)) return 0;
+            if (kind == 1 && pos_[x->op] >= 0) fen_add(pos_[x->op], 1);
+            bits[x->op >> 6] |= (1ULL << (x->op & 63));
+            const uint64_t nh = bits_hash ^ zob_[x->op];
+            *kind_out = kind;
+            if (!remember(bits, nh, state)) {
+                bits[x->op >> 6] &= ~(1ULL << (x->op & 63));
+                undo(state, kind, popped);
+                if (kind == 1 && pos_[x->op] >= 0) fen_add(pos_[x->op], -1);
+                return 2;
+            }
+            stack.push_back({x, kind, popped, -1});
+            bits_hash = nh;
+            lift(x);
+            return 1;
+        };
+        auto dominant = [&](Event* x) {
+            const Op& o = ops_[x->op];
+            if (o.noop || (o.is_enq && !o.ok)) return true;
+            if (o.is_enq) return false;
+            if (!o.ok) return state.empty();
+            return !state.empty() && state.front() == o.val;
+        };
         while (head_.next != nullptr) {
             if ((++iters & 0xFFF) == 0) {
                 double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
                 if (el > timeout_s) return 2;
             }
-            if (!backtrack && e != nullptr && e->is_call) {
-                const Op& o = ops_[e->op];
-                int kind = 0;
-                uint64_t popped = (!state.empty()) ? state.front() : 0;
-                const bool allowed = !(o.is_enq && o.ok && !o.noop) || order_ok(e->op);
-                if (allowed && model_step(state, o, &kind)) {
-                    if (kind == 1 && pos_[e->op] >= 0) fen_add(pos_[e->op], 1);
-                    bits[e->op >> 6] |= (1ULL << (e->op & 63));
-                    uint64_t nh = bits_hash ^ zob_[e->op];
-                    if (remember(bits, nh, state)) {
-                        stack.push_back({e, kind, popped});
-                        bits_hash = nh;
-                        lift(e);
-                        e = head_.next;
-                        continue;
-                    }
-                    // configuration explored before (and failed): undo the step
-                    bits[e->op >> 6] &= ~(1ULL << (e->op & 63));
-                    undo(state, kind, popped);
-                    if (kind == 1 && pos_[e->op] >= 0) fen_add(pos_[e->op], -1);
-                    if (kind != 1) { backtrack = true; continue; }   // dominated: skip alternatives
+            if (backtrack) {
+                backtrack = false;
+                for (;;) {
+                    if (stack.empty()) return 1;
+                    Frame f = stack.back();
+                    stack.pop_back();
+                    undo(state, f.kind, f.val);
+                    if (f.kind == 1 && pos_[f.call->op] >= 0) fen_add(pos_[f.call->op], -1);
+                    bits[f.call->op >> 6] &= ~(1ULL << (f.call->op & 63));
+                    bits_hash ^= zob_[f.call->op];
+                    unlift(f.call);
+                    if (f.kind == 1) { next_cand = f.cand + 1; fresh = false; break; }
                 }
-                e = e->next;
                 continue;
             }
-            // Backtrack: pop choices until one that is not a dominant no-op.
-            backtrack = false;
-            for (;;) {
-                if (stack.empty()) return 1;
-                Frame f = stack.back();
-                stack.pop_back();
-                undo(state, f.kind, f.val);
-                if (f.kind == 1 && pos_[f.call->op] >= 0) fen_add(pos_[f.call->op], -1);
-                bits[f.call->op >> 6] &= ~(1ULL << (f.call->op & 63));
-                bits_hash ^= zob_[f.call->op];
-                unlift(f.call);
-                if (f.kind == 1) { e = f.call->next; break; }   // only enqueues branch
+            if (fresh) {
+                // dominant operations among those already called
+                bool took = false;
+                for (Event* x = head_.next; x && x->is_call; x = x->next) {
+                    if (!dominant(x)) continue;
+                    int kind = 0;
+                    const int r = take(x, &kind);
+                    if (r == 1) { took = true; break; }
+                    if (r == 2) { backtrack = true; break; }
+                }
+                if (backtrack || took) continue;
+                fresh = false;
+                next_cand = 0;
             }
+            // Branch on an enqueue among those already called, earliest deadline
+            // first: the queue order must follow the dequeue order, so the value
+            // whose dequeue returns first is the most likely next one.  The order is
+            // a heuristic only; backtracking still tries every candidate.
+            cands.clear();
+            Event* first_ret = head_.next;
+            while (first_ret && first_ret->is_call) first_ret = first_ret->next;
+            const Op* due = first_ret ? &ops_[first_ret->op] : nullptr;
+            if (distinct_ && due && !due->is_enq && !due->noop) {
+                // The operation whose return comes next is a dequeue that is not
+                // dominant now.  An "empty" needs an empty queue and a valued
+                // dequeue needs its value at the head; adding enqueues helps only
+                // if the queue is empty and the dequeue's own value goes in next.
+                if (!due->ok || !state.empty()) { backtrack = true; continue; }
+                for (Event* x = head_.next; x && x->is_call; x = x->next) {
+                    const Op& o = ops_[x->op];
+                    if (o.is_enq && o.ok && !o.noop && o.val == due->val) cands.push_back(x);
+                }
+            } else {
+                for (Event* x = head_.next; x && x->is_call; x = x->next) {
+                    const Op& o = ops_[x->op];
+                    if (o.is_enq && o.ok && !o.noop) cands.push_back(x);
+                }
+            }
+            std::stable_sort(cands.begin(), cands.end(),
+                             [&](const Event* a, const Event* b) { return deadline_[a->op] < deadline_[b->op]; });
+            bool took = false;
+            for (int ci = next_cand; ci < (int)cands.size(); ++ci) {
+                int kind = 0;
+                const int r = take(cands[ci], &kind);
+                if (r == 1) { stack.back().cand = ci; took = true; break; }
+            }
+            if (took) { fresh = true; continue; }
+            backtrack = true;   // no enqueue can go next: undo the last choice
         }
         return 0;
     }
@@ -243,6 +303,7 @@ private:
         const int n = (int)ops_.size();
         need_.assign(n, 0);
         pos_.assign(n, -1);
+        deadline_.assign(n, std::numeric_limits<int64_t>::max());
         std::unordered_map<uint64_t, int> enq_of, deq_of;
         distinct_ = true;
         for (int i = 0; i < n; ++i) {
@@ -268,6 +329,7 @@ private:
             const int e = kv.second;
             auto d = deq_of.find(kv.first);
             if (d == deq_of.end()) { need_[e] = ndeq_; continue; }
+            deadline_[e] = ret[d->second];
             need_[e] = (int)(std::lower_bound(end_times.begin(), end_times.end(), call[d->second]) - end_times.begin());
         }
         fen_.assign(ndeq_ + 1, 0);
@@ -318,6 +380,7 @@ private:
     bool distinct_ = false;
     int ndeq_ = 0;
     std::vector<int> need_, pos_, fen_;
+    std::vector<int64_t> deadline_;
 };
 
 // ------------------------------------------------------------------------------

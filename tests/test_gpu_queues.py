@@ -44,9 +44,22 @@ def test_history_larger(gcq, oracle_lib, kind, threads, block):
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("pct", [25, 50, 75])
 def test_history_split(gcq, oracle_lib, kind, pct):
-    with gcq.Queue(kind, 15, 256) as q:
-        recs = q.history(threads=256, ops=16, block=128, mode=1, producer_percent=pct)
-        _lin(oracle_lib, recs)
+    # split mode at a size the exact search decides (it is exponential in the number
+    # of concurrent producers in the worst case, like the reference's checker)
+    with gcq.Queue(kind, 15, 32) as q:
+        for rep in range(3):
+            recs = q.history(threads=32, ops=16, block=32, mode=1, producer_percent=pct)
+            _lin(oracle_lib, recs)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_history_split_large_patterns(gcq, oracle_lib, kind):
+    # 1024 threads: the O(n log n) pattern scan (sound; complete when no dequeue
+    # reports empty) must find no violation
+    with gcq.Queue(kind, 15, 1024) as q:
+        recs = q.history(threads=1024, ops=16, block=256, mode=1, producer_percent=50)
+        rep = oracle_lib.patterns(recs)
+        assert not rep["violations"], rep
 
 
 @pytest.mark.parametrize("kind", ["gwfq", "glfq"])
@@ -56,7 +69,7 @@ def test_history_small_ring_wraps(gcq, oracle_lib, kind):
         for rep in range(3):
             recs = q.history(threads=64, ops=64, block=64)
             _lin(oracle_lib, recs)
-            recs = q.history(threads=64, ops=64, block=64, mode=1, producer_percent=50)
+            recs = q.history(threads=16, ops=32, block=32, mode=1, producer_percent=50)
             _lin(oracle_lib, recs)
 
 
@@ -68,7 +81,7 @@ def test_gwfq_slow_path_and_helping(gcq, oracle_lib):
         for rep in range(3):
             recs = q.history(threads=128, ops=32, block=128)
             _lin(oracle_lib, recs)
-            recs = q.history(threads=128, ops=32, block=64, mode=1, producer_percent=50)
+            recs = q.history(threads=32, ops=16, block=32, mode=1, producer_percent=50)
             _lin(oracle_lib, recs)
         assert q.error_word() == 0
 

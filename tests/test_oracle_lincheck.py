@@ -189,3 +189,74 @@ def test_search_with_distinct_values_agrees_with_brute_force(oracle_lib):
         assert oracle_lib.check(a) == ("Linearizable (FIFO)" if want else "Not linearizable (FIFO)"), h
         counts[want] += 1
     assert counts[True] > 40 and counts[False] > 40, counts
+
+
+def synthetic_history(rng, producers, consumers, ops_per_thread, overlap=40):
+    """A history that is linearizable by construction: every operation gets an
+    interval and a linearisation point inside it, and the results come from a real
+    FIFO applied in point order.  Producers/consumers run back to back with long,
+    overlapping intervals, so there are many concurrent "empty" dequeues."""
+    ops = []
+    for p in range(producers + consumers):
+        t = rng.randint(0, overlap)
+        for i in range(ops_per_thread):
+            call = t
+            end = call + rng.randint(1, overlap)
+            lin = rng.uniform(call, end)
+            kind = 0 if p < producers else 1
+            val = (p << 32) | (i + 1)
+            ops.append([lin, p, kind, val, call, end])
+            t = end + rng.randint(0, overlap // 4)
+    ops.sort()
+    q, recs = [], []
+    for lin, p, kind, val, call, end in ops:
+        if kind == 0:
+            q.append(val)
+            recs.append(dict(proc=p, op=0, arg=val, ret=1, call=call, end=end))
+        else:
+            ret = q.pop(0) if q else 0
+            recs.append(dict(proc=p, op=1, arg=0, ret=ret, call=call, end=end))
+    # distinct logical timestamps: spread ties deterministically
+    stamps = sorted({(r["call"], 0, i) for i, r in enumerate(recs)} | {(r["end"], 1, i) for i, r in enumerate(recs)})
+    for k, (_, is_end, i) in enumerate(stamps):
+        recs[i]["end" if is_end else "call"] = k + 1
+    # ties resolved call-before-end only within equal times; keep call < end per op
+    for r in recs:
+        assert r["call"] < r["end"]
+    return recs
+
+
+@pytest.mark.parametrize("producers,consumers,ops", [(8, 24, 16), (8, 24, 6), (48, 16, 16), (4, 60, 8)])
+def test_synthetic_split_histories(oracle_lib, producers, consumers, ops):
+    """Exact verdicts on split-mode-like histories at the sizes the split GPU tests
+    use.  (The exact search is exponential in the worst case, like the reference's
+    Porcupine search; much larger split histories can end "Unknown (timeout)".)"""
+    import time
+    rng = random.Random(producers * 1000 + consumers)
+    for it in range(5):
+        recs = synthetic_history(rng, producers, consumers, ops)
+        a = oracle_lib.records_from_dicts(recs)
+        t0 = time.time()
+        assert oracle_lib.check(a, timeout_s=30) == "Linearizable (FIFO)"
+        assert time.time() - t0 < 10
+
+
+@pytest.mark.parametrize("producers,consumers,ops", [(64, 192, 16), (256, 256, 16)])
+def test_synthetic_large_patterns(oracle_lib, producers, consumers, ops):
+    """Large histories: the pattern scan finds nothing in a linearizable history and
+    flags a swapped pair of dequeues."""
+    rng = random.Random(producers)
+    recs = synthetic_history(rng, producers, consumers, ops)
+    a = oracle_lib.records_from_dicts(recs)
+    assert not oracle_lib.patterns(a)["violations"]
+    deqs = [i for i, r in enumerate(recs) if r["op"] == 1 and r["ret"]]
+    by_val = {r["arg"]: r for r in recs if r["op"] == 0}
+    for i in deqs:
+        for j in deqs:
+            if recs[i]["end"] < recs[j]["call"] and by_val[recs[i]["ret"]]["end"] < by_val[recs[j]["ret"]]["call"]:
+                recs[i]["ret"], recs[j]["ret"] = recs[j]["ret"], recs[i]["ret"]
+                b = oracle_lib.records_from_dicts(recs)
+                assert oracle_lib.patterns(b)["order"] >= 1
+                assert oracle_lib.check(b) == "Not linearizable (FIFO)"
+                return
+    pytest.fail("no swappable pair")
