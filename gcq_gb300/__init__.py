@@ -85,6 +85,7 @@ SIGNATURES = {
     "gcq_tb_run": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
     "gcq_fifo_check": ([P, U32, U32, U32, C.POINTER(FifoResult)], I32),
     "gcq_roofline_measure": ([C.POINTER(Roofline), I32], I32),
+    "gcq_tb_chunk_host_noalloc": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
 }
 
 _LIB = None
@@ -200,6 +201,16 @@ class Queue:
         c = TbCounters()
         _check(_lib().gcq_tb_chunk_host(self._h, mode, producer_percent, threads, block, chunk_ops,
                                         payloads.ctypes.data, C.byref(c), P(stream)), "gcq_tb_chunk_host")
+        return {f: getattr(c, f) for f, _ in TbCounters._fields_}
+
+    def tb_chunk_host_noalloc(self, mode: int, threads: int, chunk_ops: int, payloads: np.ndarray,
+                              block: int = 256, producer_percent: int = 50, stream: int = 0) -> dict:
+        """gcq_tb_chunk_host without device allocation (fixed staging in libgcq.so)."""
+        assert payloads.dtype == np.uint32 and payloads.size == threads * chunk_ops
+        c = TbCounters()
+        _check(_lib().gcq_tb_chunk_host_noalloc(self._h, mode, producer_percent, threads, block, chunk_ops,
+                                                payloads.ctypes.data, C.byref(c), P(stream)),
+               "gcq_tb_chunk_host_noalloc")
         return {f: getattr(c, f) for f, _ in TbCounters._fields_}
 
     def tb_run(self, mode: int, threads: int, chunk_ops: int = 128, block: int = 256, producer_percent: int = 50,

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gcq_internal.cuh"
@@ -474,3 +475,64 @@ int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ no-allocation chunk
+// gcq_tb_chunk_host_noalloc: the end-to-end chunk of gcq_tb_chunk_host for callers
+// that must not allocate device memory during the call, with its device staging in
+// a fixed array of this file instead of a cudaMalloc'd buffer.
+namespace {
+
+// 16 MiB of payload staging (GCQ_NOALLOC_MAX_PAYLOADS uint32 values) followed by one
+// 256-byte block for the counters.  Every GPU that loads the library holds it until
+// the process exits.
+constexpr uint64_t kNoallocPayloadWords = GCQ_NOALLOC_MAX_PAYLOADS;
+constexpr uint64_t kNoallocWords = kNoallocPayloadWords + 64;
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoallocWords];
+
+// Device address of g_noalloc_scratch, looked up once per device.  In host code the
+// array's name stands for a host-side shadow, not a device address, so it must never
+// be passed to a kernel; cudaGetSymbolAddress gives the address on the current device.
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    GCQ_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return GCQ_EUNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        GCQ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (!p) return GCQ_ECUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return GCQ_OK;
+}
+
+}  // namespace
+
+extern "C" int gcq_tb_chunk_host_noalloc(gcq_queue* q, int mode, int producer_percent, uint32_t threads,
+                                         uint32_t block, uint32_t chunk_ops, const uint32_t* host_payloads,
+                                         gcq_tb_counters* host_counters, void* stream) {
+    int rc = check_tb_args(q, mode, producer_percent, threads, block, chunk_ops);
+    if (rc != GCQ_OK) return rc;
+    if (!host_payloads || !host_counters) return GCQ_EINVAL;
+    if ((uint64_t)threads * chunk_ops > kNoallocPayloadWords) return GCQ_ECAPACITY;
+    void* base = nullptr;
+    rc = noalloc_scratch(&base);
+    if (rc != GCQ_OK) return rc;
+    cudaStream_t s = gcqi::as_stream(stream);
+    uint32_t* d_pay = (uint32_t*)base;
+    gcq_tb_counters* d_ctr = (gcq_tb_counters*)((uint32_t*)base + kNoallocPayloadWords);
+    const size_t pbytes = (size_t)threads * chunk_ops * sizeof(uint32_t);
+    GCQ_CUDA(cudaMemcpyAsync(d_pay, host_payloads, pbytes, cudaMemcpyHostToDevice, s));
+    // the array keeps the previous call's counters: clear them before the kernel adds
+    GCQ_CUDA(cudaMemsetAsync(d_ctr, 0, sizeof(gcq_tb_counters), s));
+    rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, d_pay, d_ctr, s);
+    if (rc != GCQ_OK) return rc;
+    GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
+    GCQ_CUDA(cudaStreamSynchronize(s));
+    return GCQ_OK;
+}

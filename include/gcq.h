@@ -146,6 +146,26 @@ int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t thr
                       uint32_t chunk_ops, const uint32_t* host_payloads, gcq_tb_counters* host_counters,
                       void* stream);
 
+/* Capacity of gcq_tb_chunk_host_noalloc: payloads per call (16 MiB of uint32). */
+#define GCQ_NOALLOC_MAX_PAYLOADS (4u * 1024u * 1024u)
+
+/* No counterpart in the reference.  gcq_tb_chunk_host without any device
+ * allocation, for callers that cannot call cudaMalloc while they run: code inside a
+ * stream-ordered or pool-managed memory regime, real-time callers that may not take
+ * the allocator's locks or synchronisation, and embedders that own all device
+ * memory.  The payload staging and the counters live in a fixed 16 MiB + 256 B
+ * array compiled into libgcq.so (GCQ_NOALLOC_MAX_PAYLOADS payloads; larger
+ * threads * chunk_ops returns GCQ_ECAPACITY).  Every GPU that loads the library
+ * holds that array until the process exits.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) and caches it; make that first
+ * call before any stream capture.  All calls share the one array: the counters are
+ * cleared at the start of every call, and calls whose work overlaps on the GPU (on
+ * different streams, or from different host threads) race on it.  Arguments and
+ * results are those of gcq_tb_chunk_host. */
+int gcq_tb_chunk_host_noalloc(gcq_queue* q, int mode, int producer_percent, uint32_t threads,
+                              uint32_t block, uint32_t chunk_ops, const uint32_t* host_payloads,
+                              gcq_tb_counters* host_counters, void* stream);
+
 typedef struct gcq_tb_result {
     gcq_tb_counters counters;
     double gpu_ms;       /* CUDA-event time of the timed window */
