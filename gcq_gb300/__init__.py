@@ -14,7 +14,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libgcq.so")
+# GCQ_LIBRARY_PATH selects another build of the same library (e.g. a tuning variant)
+LIB_PATH = os.environ.get("GCQ_LIBRARY_PATH") or os.path.join(HERE, "_build", "libgcq.so")
 
 KINDS = {"gwfq": 0, "glfq": 1, "wfq": 2, "sfq": 3}
 KIND_NAMES = {v: k for k, v in KINDS.items()}
@@ -31,7 +32,7 @@ LOG_DTYPE = np.dtype([("proc", "<u8"), ("op", "<u4"), ("_pad", "<u4"), ("arg", "
 class Knobs(C.Structure):
     _fields_ = [("help_delay", C.c_uint32), ("enq_patience", C.c_uint32), ("deq_patience", C.c_uint32),
                 ("remap", C.c_uint32), ("ymc_patience", C.c_uint32), ("ymc_ops_per_thread", C.c_uint32),
-                ("wait_timeout_ns", C.c_uint64)]
+                ("wait_timeout_ns", C.c_uint64), ("deq_wait", C.c_uint32), ("_pad", C.c_uint32)]
 
 
 class TbCounters(C.Structure):
@@ -54,6 +55,12 @@ class Roofline(C.Structure):
     _fields_ = [("r1_single", C.c_double), ("r1_warp", C.c_double), ("rs_lines", C.c_double),
                 ("rs_contig", C.c_double), ("rc_lines", C.c_double), ("rc128_lines", C.c_double),
                 ("hbm_gbs", C.c_double), ("sms", C.c_int), ("_pad", C.c_int)]
+
+
+class BfsResult(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("kernel_ms", C.c_double), ("init_ms", C.c_double),
+                ("edges_scanned", C.c_uint64), ("reached", C.c_uint32), ("levels", C.c_int32),
+                ("max_frontier", C.c_uint32), ("drops", C.c_uint32)]
 
 
 class GcqError(RuntimeError):
@@ -85,7 +92,14 @@ SIGNATURES = {
     "gcq_tb_run": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
     "gcq_fifo_check": ([P, U32, U32, U32, C.POINTER(FifoResult)], I32),
     "gcq_roofline_measure": ([C.POINTER(Roofline), I32], I32),
+    "gcq_stats": ([P, C.POINTER(C.c_uint64), I32], I32),
     "gcq_tb_chunk_host_noalloc": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
+    "gcq_graph_grid": ([U32, U32, C.c_double, C.c_double, U64, C.POINTER(P), C.POINTER(P),
+                        C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
+    "gcq_free": ([P], None),
+    "gcq_bfs_create": ([I32, P, P, C.c_int32, C.c_int64, U32, U32, C.POINTER(Knobs), C.POINTER(P)], I32),
+    "gcq_bfs_destroy": ([P], I32),
+    "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
 }
 
 _LIB = None
@@ -179,6 +193,15 @@ class Queue:
         _check(_lib().gcq_error_word(self._h, C.byref(e), int(clear)), "gcq_error_word")
         return e.value
 
+    STAT_NAMES = ["try_enq", "try_deq", "deq_retry", "enq_slow", "deq_slow", "finalize",
+                  "finalize_scan", "deq_waited"]
+
+    def stats(self, clear: bool = False) -> dict:
+        """G-WFQ operation counters per ring (non-zero only in GCQ_STATS builds)."""
+        a = (C.c_uint64 * 16)()
+        _check(_lib().gcq_stats(self._h, a, int(clear)), "gcq_stats")
+        return {ring: dict(zip(self.STAT_NAMES, list(a)[i * 8:(i + 1) * 8])) for i, ring in enumerate(["aq", "fq"])}
+
     # --- history harness -------------------------------------------------------
     def history(self, threads: int, ops: int, block: int = 256, mode: int = 0, producer_percent: int = 50,
                 value_mode: int = 0, stream: int = 0) -> np.ndarray:
@@ -234,6 +257,62 @@ class Queue:
         r = FifoResult()
         _check(_lib().gcq_fifo_check(self._h, threads, block, ops_per_thread, C.byref(r)), "gcq_fifo_check")
         return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+
+def graph_grid(rows: int, cols: int, keep_p: float = 0.6, diag_p: float = 0.01, seed: int = 1):
+    """Seeded grid graph as CSR (offsets, indices) int32 numpy arrays (gcq_graph_grid)."""
+    po, pi = P(), P()
+    V, E = C.c_int32(), C.c_int64()
+    _check(_lib().gcq_graph_grid(rows, cols, keep_p, diag_p, seed, C.byref(po), C.byref(pi),
+                                 C.byref(V), C.byref(E)), "gcq_graph_grid")
+    off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int32)), shape=(V.value + 1,)).copy()
+    idx = np.ctypeslib.as_array(C.cast(pi, C.POINTER(C.c_int32)), shape=(max(E.value, 1),))[: E.value].copy()
+    _lib().gcq_free(po)
+    _lib().gcq_free(pi)
+    return off, idx
+
+
+class Bfs:
+    """A CSR graph on the device with two frontier queues (gcq_bfs_create)."""
+
+    def __init__(self, kind: str, offsets: np.ndarray, indices: np.ndarray, threads: int = 8192,
+                 capacity_log2: int = 0, knobs: Knobs | None = None, **overrides):
+        self.off = np.ascontiguousarray(offsets, dtype=np.int32)
+        self.idx = np.ascontiguousarray(indices, dtype=np.int32)
+        self.V = len(self.off) - 1
+        k = knobs or default_knobs()
+        for name, v in overrides.items():
+            setattr(k, name, v)
+        h = P()
+        _check(_lib().gcq_bfs_create(KINDS[kind], self.off.ctypes.data, self.idx.ctypes.data, self.V,
+                                     len(self.idx), threads, capacity_log2, C.byref(k), C.byref(h)),
+               "gcq_bfs_create")
+        self._h = h
+        self.threads = threads
+
+    def run(self, src: int = 0, block: int = 256, persistent: bool = False, levels: bool = True):
+        lv = np.empty(self.V, dtype=np.int32) if levels else None
+        r = BfsResult()
+        _check(_lib().gcq_bfs_run(self._h, src, block, int(persistent), lv.ctypes.data if levels else None,
+                                  C.byref(r)), "gcq_bfs_run")
+        return {f: getattr(r, f) for f, _ in BfsResult._fields_}, lv
+
+    def close(self):
+        if self._h:
+            _lib().gcq_bfs_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def roofline(reps: int = 3) -> dict:

@@ -23,6 +23,7 @@ struct gcq_queue {
     void* obj;               // device address of the queue object
     gcq::u32a* err;          // device address of the error word
     uint64_t ymc_cells;      // YMC pool size in cells
+    gcq::u64a* stats;        // G-WFQ operation counters (2 rings x 8), device address
 };
 
 namespace gcqi {

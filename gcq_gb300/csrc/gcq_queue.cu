@@ -24,6 +24,7 @@ __global__ void k_init_gwf(gcq::gwf::mpmc* q) {
     const uint64_t n = (uint64_t)gridDim.x * blockDim.x;
     gcq::gwf::init_slice(&q->aq, false, gid, n);
     gcq::gwf::init_slice(&q->fq, true, gid, n);
+    if (gid < 2 * gcq::gwf::stat::COUNT && q->aq.stats) q->aq.stats[gid] = 0;
     if (gid == 0) *q->err = 0;
 }
 
@@ -129,6 +130,8 @@ void gcq_default_knobs(gcq_knobs* k) {
     k->ymc_patience = WF_PATIENCE;
     k->ymc_ops_per_thread = WF_PREALLOC_OPS_PER_THREAD;
     k->wait_timeout_ns = 2000000000ull;
+    k->deq_wait = 8;
+    k->_pad = 0;
 }
 
 const char* gcq_strerror(int s) {
@@ -194,6 +197,7 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
             const uint64_t o_fh = take((uint64_t)max_threads * sizeof(gcq::gwf::helper_state));
             const uint64_t o_d = take(n * 8);
             const uint64_t o_ao = take(2 * n * 4), o_fo = take(2 * n * 4);
+            const uint64_t o_st = take(2 * gcq::gwf::stat::COUNT * 8);
             q->bytes = align_up(off, A);
             if (cudaMalloc(&q->base, q->bytes) != cudaSuccess) { delete q; return GCQ_ENOMEM; }
             char* b = (char*)q->base;
@@ -212,9 +216,13 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
                 r.enq_patience = k.enq_patience;
                 r.deq_patience = k.deq_patience;
                 r.remap = k.remap ? 1u : 0u;
+                r.deq_wait = k.deq_wait;
             };
             fill(h.aq, o_ae, o_ar, o_ah, o_ao);
             fill(h.fq, o_fe, o_fr, o_fh, o_fo);
+            h.aq.stats = (gcq::u64a*)(b + o_st);
+            h.fq.stats = h.aq.stats + gcq::gwf::stat::COUNT;
+            q->stats = h.aq.stats;
             h.data = (gcq::u64a*)(b + o_d);
             h.err = (gcq::u32a*)(b + o_err);
             q->obj = b + o_hdr;
@@ -239,6 +247,7 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
             h.aq.err = h.fq.err = h.err = (gcq::u32a*)(b + o_err);
             h.aq.order = h.fq.order = capacity_log2;
             h.aq.line_log2 = h.fq.line_log2 = line_log2;
+            h.aq.deq_wait = h.fq.deq_wait = k.deq_wait;
             h.data = (gcq::u64a*)(b + o_d);
             q->obj = b + o_hdr;
             q->err = (gcq::u32a*)(b + o_err);
@@ -345,6 +354,16 @@ int gcq_error_word(gcq_queue* q, uint32_t* err, int clear) {
 }
 
 uint64_t gcq_device_bytes(const gcq_queue* q) { return q ? q->bytes : 0; }
+
+int gcq_stats(gcq_queue* q, uint64_t* out, int clear) {
+    if (!q || !out) return GCQ_EINVAL;
+    memset(out, 0, 16 * sizeof(uint64_t));
+    if (q->kind != GCQ_GWFQ || !q->stats) return GCQ_OK;
+    GCQ_CUDA(cudaDeviceSynchronize());
+    GCQ_CUDA(cudaMemcpy(out, q->stats, 16 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    if (clear) GCQ_CUDA(cudaMemset(q->stats, 0, 16 * sizeof(uint64_t)));
+    return GCQ_OK;
+}
 
 int gcq_info(const gcq_queue* q, int* kind, uint32_t* capacity_log2, uint32_t* max_threads) {
     if (!q) return GCQ_EINVAL;

@@ -56,6 +56,10 @@ typedef struct gcq_knobs {
     uint32_t ymc_patience;        /* WF_PATIENCE, wfqueue_hip_opt.hpp:29-31 (16) */
     uint32_t ymc_ops_per_thread;  /* WF_PREALLOC_OPS_PER_THREAD, wfqueue_hip_opt.hpp:33-35 (512) */
     uint64_t wait_timeout_ns;     /* deadline of one blocking wait (SFQ), default 2 s */
+    uint32_t deq_wait;            /* G-WFQ/G-LFQ: re-reads (with back-off) of a not-yet-filled
+                                     slot before a dequeuer marks it; default 8 (0 = mark at
+                                     once, as the reference does) */
+    uint32_t _pad;
 } gcq_knobs;
 
 typedef struct gcq_queue gcq_queue;
@@ -87,6 +91,12 @@ int gcq_device_ptr(gcq_queue* q, void** dev);
 int gcq_error_word(gcq_queue* q, uint32_t* err, int clear);
 /* Bytes of device memory held by the queue. */
 uint64_t gcq_device_bytes(const gcq_queue* q);
+/* G-WFQ operation counters per ring (aq then fq, 8 each: fast-path enqueue
+ * attempts, dequeue attempts, dequeue retries, slow enqueues, slow dequeues,
+ * finalize calls, finalize record scans, dequeues served by waiting).  Counted only
+ * when libgcq.so is built with GCQ_STATS=1 (the reference's GWF_PROFILE counters,
+ * gwf_ring.hpp:23-36); otherwise all zero.  out must hold 16 values. */
+int gcq_stats(gcq_queue* q, uint64_t* out, int clear);
 /* Kind, capacity_log2 and max_threads the queue was created with. */
 int gcq_info(const gcq_queue* q, int* kind, uint32_t* capacity_log2, uint32_t* max_threads);
 const char* gcq_strerror(int status);
@@ -199,6 +209,47 @@ typedef struct gcq_fifo_result {
 
 int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
                    gcq_fifo_result* out);
+
+/* ------------------------------------------------------------------ BFS ----
+ * Level-synchronous BFS with a queue as the frontier (concurrent_bfs/bfs_bench.cpp). */
+typedef struct gcq_bfs_ctx gcq_bfs_ctx;
+
+typedef struct gcq_bfs_result {
+    double total_ms;          /* host time of the whole traversal, init included */
+    double kernel_ms;         /* CUDA-event time of the level kernels */
+    double init_ms;           /* reset of levels and queues + source enqueue */
+    uint64_t edges_scanned;
+    uint32_t reached;         /* vertices with a level, the source included */
+    int32_t levels;           /* BFS levels processed (the last one finds nothing) */
+    uint32_t max_frontier;
+    uint32_t drops;           /* enqueues refused because the frontier outgrew the queue */
+} gcq_bfs_result;
+
+/* Seeded grid graph: vertex r*cols+c; each right/down edge kept with probability
+ * keep_p; from each vertex, with probability diag_p, one diagonal shortcut to the
+ * next row.  Undirected CSR (neighbours ascending), arrays from malloc (free them
+ * with gcq_free).  With keep_p = 1 and diag_p = 0 it is build_grid of
+ * bfs_bench.cpp:245-256. */
+int gcq_graph_grid(uint32_t rows, uint32_t cols, double keep_p, double diag_p, uint64_t seed,
+                   int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
+void gcq_free(void* p);
+
+/* Upload the CSR and create the two frontier queues of `kind` for `threads`
+ * worker threads (a multiple of 32) with capacity 2^capacity_log2 (0 = the
+ * smallest power of two >= V, at least 2^15, within the queue's envelope).
+ * Replaces bfs_bench.cpp:702-737. */
+int gcq_bfs_create(int kind, const int32_t* offsets, const int32_t* indices, int32_t V, int64_t E,
+                   uint32_t threads, uint32_t capacity_log2, const gcq_knobs* knobs, gcq_bfs_ctx** out);
+int gcq_bfs_destroy(gcq_bfs_ctx* c);
+
+/* One traversal from src (run_bfs, bfs_bench.cpp:509-633).  persistent = 0 launches
+ * bfs_expand_kernel + bfs_hub_kernel per level and reads the next frontier size on
+ * the host, as the reference does; persistent = 1 runs every level in one
+ * cooperative launch with grid barriers.  host_levels (V entries, may be NULL)
+ * receives the depths, -1 for unreached vertices.  A frontier larger than the queue
+ * returns GCQ_ECAPACITY (the reference drops the vertices silently). */
+int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int32_t* host_levels,
+                gcq_bfs_result* out);
 
 /* ------------------------------------------------------------- roofline ----
  * The atomic roofline of this GPU, measured by a microbenchmark in the same

@@ -5,10 +5,12 @@
 // (gwf_ring.hpp:15-17) and on __threadfence for publication.  On NVIDIA GPUs plain
 // atomicCAS/atomicAdd are relaxed, so every shared queue word here goes through an
 // explicitly ordered PTX operation at .gpu scope:
-//   * read-modify-writes on entries, counters and request records are acq_rel;
-//   * loads of shared words are acquire (entries, counters) or relaxed (hints that
-//     a following CAS validates);
-//   * publication stores are release;
+//   * the fast paths use the weakest order each step needs: relaxed tickets and
+//     entry loads, a release CAS where an enqueue publishes (it makes the payload
+//     written before it visible), an acquire OR where a dequeue consumes (it makes
+//     the payload visible to the reads after it), relaxed marking CASes;
+//   * the slow paths and request records keep acq_rel read-modify-writes and
+//     acquire/release loads and stores;
 //   * the two store->load (Dekker) points of the SCQ emptiness argument get a
 //     fence.sc (GCQ_SC_FENCES, on by default): a dequeuer's read of Tail after its
 //     fetch-and-add on Head, and an enqueuer's read of Head after its add on Tail.
@@ -130,6 +132,35 @@ __device__ __forceinline__ uint32_t cas(u32a* p, uint32_t expect, uint32_t desir
                  : "=r"(old) : "l"(p), "r"(expect), "r"(desired) : "memory");
     return old;
 }
+__device__ __forceinline__ uint64_t cas_rel(u64a* p, uint64_t expect, uint64_t desired) {
+    uint64_t old;
+    asm volatile("atom.release.gpu.global.cas.b64 %0, [%1], %2, %3;"
+                 : "=l"(old) : "l"(p), "l"(expect), "l"(desired) : "memory");
+    return old;
+}
+__device__ __forceinline__ uint64_t cas_rlx(u64a* p, uint64_t expect, uint64_t desired) {
+    uint64_t old;
+    asm volatile("atom.relaxed.gpu.global.cas.b64 %0, [%1], %2, %3;"
+                 : "=l"(old) : "l"(p), "l"(expect), "l"(desired) : "memory");
+    return old;
+}
+__device__ __forceinline__ bool cas_upd_rel(u64a* p, uint64_t* expect, uint64_t desired) {
+    const uint64_t old = cas_rel(p, *expect, desired);
+    const bool ok = (old == *expect);
+    *expect = old;
+    return ok;
+}
+__device__ __forceinline__ bool cas_upd_rlx(u64a* p, uint64_t* expect, uint64_t desired) {
+    const uint64_t old = cas_rlx(p, *expect, desired);
+    const bool ok = (old == *expect);
+    *expect = old;
+    return ok;
+}
+__device__ __forceinline__ uint64_t fetch_or_acq(u64a* p, uint64_t v) {
+    uint64_t old;
+    asm volatile("atom.acquire.gpu.global.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
+}
 // CAS that reports success and refreshes `expect` with the observed value
 // (the C11 compare_exchange contract used by gwf_ring.hpp:93-99).
 __device__ __forceinline__ bool cas_upd(u64a* p, uint64_t* expect, uint64_t desired) {
@@ -204,6 +235,19 @@ __device__ __forceinline__ uint64_t warp_fetch_add(u64a* p, uint64_t step) {
     const unsigned rank = __popc(peers & lanemask_lt());
     uint64_t base = 0;
     if ((int)lane_id() == leader) base = fetch_add(p, step * (uint64_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint64_t)rank * step;
+}
+// The same with a relaxed fetch-and-add: a ticket orders nothing by itself (the
+// entry it selects is read through its address), so the fast paths take their
+// tickets without a fence; the store->load points have their own fence.sc.
+__device__ __forceinline__ uint64_t warp_ticket(u64a* p, uint64_t step) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, (unsigned long long)(uintptr_t)p);
+    const int leader = __ffs(peers) - 1;
+    const unsigned rank = __popc(peers & lanemask_lt());
+    uint64_t base = 0;
+    if ((int)lane_id() == leader) base = fetch_add_rlx(p, step * (uint64_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
     return base + (uint64_t)rank * step;
 }

@@ -6,6 +6,9 @@
 // indirection layout (:126-138), enqueue/dequeue loops (:467-560), 64-bit payload
 // indirection (:566-582).
 // Changed for GB300: ring capacity and the permutation are runtime header fields;
+// the enqueue CAS is tried first against the steady-state free slot, and a
+// dequeuer waits briefly for the enqueuer holding its ticket before marking the
+// slot (deq_wait);
 // the permutation spreads over 128-byte lines (16 entries) by default; Tail, Head
 // and Threshold own separate lines; loads are acquire/relaxed loads instead of
 // atomicAdd(p, 0) (:144-148); retry loops are bounded (GCQ_SPIN_LIMIT) and report
@@ -59,7 +62,8 @@ struct alignas(128) ring {
     u32a* err;
     uint32_t order;       // log2 N
     uint32_t line_log2;   // log2 entries per line for the permutation; 0 = identity
-    char _pad3[104];
+    uint32_t deq_wait;    // re-reads of a not-yet-filled slot before marking it
+    char _pad3[100];
 };
 
 struct alignas(128) mpmc {
@@ -72,7 +76,7 @@ struct alignas(128) mpmc {
 struct cfg {
     u64a* entry;
     u32a* err;
-    uint32_t order, line_log2;
+    uint32_t order, line_log2, deq_wait;
     __host__ __device__ __forceinline__ uint32_t slots() const { return 2u << order; }
     __host__ __device__ __forceinline__ int32_t threshold_max() const { return 3 * (int32_t)(1u << order) - 1; }
     __host__ __device__ __forceinline__ uint32_t cycle_of(uint64_t t) const { return (uint32_t)(t >> (order + 1)) & CYCLE_MASK; }
@@ -93,6 +97,7 @@ struct cfg {
 __device__ __forceinline__ cfg load_cfg(const ring* q) {
     cfg c;
     c.entry = q->Entry; c.err = q->err; c.order = q->order; c.line_log2 = q->line_log2;
+    c.deq_wait = q->deq_wait;
     return c;
 }
 
@@ -127,18 +132,24 @@ __device__ inline void catchup(ring* q, uint64_t tail, uint64_t head) {
 __device__ inline bool enqueue(ring* q, uint32_t index) {
     const cfg c = load_cfg(q);
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
-        const uint64_t T = warp_fetch_add(&q->Tail, 1);
+        const uint64_t T = warp_ticket(&q->Tail, 1);
         const uint32_t tcyc = c.cycle_of(T);
         const uint32_t j = c.slot_of(T);
-        uint64_t E = ld_rlx(&c.entry[j]);
+        // CAS first against the steady-state free slot (previous cycle, safe,
+        // consumed); a mismatch returns the current value for the loop below.
+        uint64_t E = ent::pack(tcyc - 1, true, BOT_C);
+        if (cas_upd_rel(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
+            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            return true;
+        }
         for (;; ++spin) {
             const uint32_t ecyc = ent::cycle(E), eidx = ent::index(E);
             if (cycle_cmp(ecyc, tcyc) >= 0 || eidx < BOT) break;
             if (!ent::safe(E)) {
                 dekker_fence();
-                if (ld_acq(&q->Head) > T) break;
+                if (ld_rlx(&q->Head) > T) break;
             }
-            if (!cas_upd(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
+            if (!cas_upd_rel(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
                 if (spin >= GCQ_SPIN_LIMIT) break;
                 continue;
             }
@@ -152,25 +163,35 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
 
 // fq_dequeue, glf_queue.hpp:510-560.  Returns the index or BOT when empty.
 __device__ inline uint32_t dequeue(ring* q) {
-    if (ld_acq(&q->Threshold) < 0) return BOT;
+    if (ld_rlx(&q->Threshold) < 0) return BOT;
     const cfg c = load_cfg(q);
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
-        const uint64_t H = warp_fetch_add(&q->Head, 1);
+        const uint64_t H = warp_ticket(&q->Head, 1);
         const uint32_t hcyc = c.cycle_of(H);
         const uint32_t j = c.slot_of(H);
-        uint64_t E = ld_acq(&c.entry[j]);
+        uint64_t E = ld_rlx(&c.entry[j]);
+        // bounded wait for the enqueuer holding this ticket (see gwf::try_deq)
+        if (c.deq_wait && cycle_cmp(ent::cycle(E), hcyc) < 0 && ent::index(E) >= BOT) {
+            uint32_t ns = 32;
+            for (uint32_t w = 0; w < c.deq_wait; ++w) {
+                __nanosleep(ns);
+                ns = ns < 1024 ? ns * 2 : ns;
+                E = ld_rlx(&c.entry[j]);
+                if (!(cycle_cmp(ent::cycle(E), hcyc) < 0 && ent::index(E) >= BOT)) break;
+            }
+        }
         for (;; ++spin) {
             const uint32_t ecyc = ent::cycle(E), eidx = ent::index(E);
             if (cycle_cmp(ecyc, hcyc) == 0 && eidx < BOT) {
-                fetch_or(&c.entry[j], ent::CONSUME_MASK);
+                fetch_or_acq(&c.entry[j], ent::CONSUME_MASK);   // acquire: payload reads follow
                 return eidx;
             }
             if (cycle_cmp(ecyc, hcyc) >= 0 || spin >= GCQ_SPIN_LIMIT) break;
             const uint64_t nw = (eidx >= BOT) ? ent::pack(hcyc, ent::safe(E), BOT) : ent::pack(ecyc, false, eidx);
-            if (cas_upd(&c.entry[j], &E, nw)) break;
+            if (cas_upd_rlx(&c.entry[j], &E, nw)) break;
         }
         dekker_fence();
-        const uint64_t T = ld_acq(&q->Tail);
+        const uint64_t T = ld_rlx(&q->Tail);
         if (T <= H + 1) {
             catchup(q, T, H + 1);
             fetch_add(&q->Threshold, -1);

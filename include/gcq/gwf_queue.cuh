@@ -81,6 +81,31 @@ namespace local {
 constexpr uint64_t FIN = 1, INC = 2, CNT_MASK = ~3ULL;
 }
 
+// Operation counters of a ring, kept when the library is built with GCQ_STATS=1
+// (the reference's GWF_PROFILE counters, gwf_ring.hpp:23-36, which it declares
+// but never defines).
+namespace stat {
+enum : int {
+    TRY_ENQ = 0,      // fast-path enqueue attempts
+    TRY_DEQ = 1,      // fast-path dequeue attempts
+    DEQ_RETRY = 2,    // fast-path dequeue attempts that found nothing and retried
+    ENQ_SLOW = 3,     // enqueues that entered the slow path
+    DEQ_SLOW = 4,     // dequeues that entered the slow path
+    FINALIZE = 5,     // finalize_request calls (consumed Enq=0 entries)
+    FINALIZE_SCAN = 6,// finalize_request calls that fell back to the record scan
+    DEQ_WAITED = 7,   // dequeues that found their slot filled while waiting for it
+    COUNT = 8
+};
+}
+#ifndef GCQ_STATS
+#define GCQ_STATS 0
+#endif
+#if GCQ_STATS
+#define GCQ_STAT(c, k) do { if ((c).stats) atomicAdd((unsigned long long*)&(c).stats[k], 1ull); } while (0)
+#else
+#define GCQ_STAT(c, k) do { } while (0)
+#endif
+
 // Shared part of a thread's record: help request + phase-2 record, one 128-B line.
 struct alignas(128) record {
     u32a seq1, enqueue, pending, index;
@@ -119,6 +144,9 @@ struct alignas(128) ring {
     uint32_t max_threads;   // number of records; thread indices must be below it
     uint32_t help_delay, enq_patience, deq_patience;
     uint32_t remap;         // 1: spread consecutive tickets over different lines
+    uint32_t deq_wait;      // re-reads of a not-yet-filled slot before marking it
+    uint32_t _pad4;
+    u64a* stats;            // operation counters (GCQ_STATS builds), see stat::
 };
 
 // Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345).
@@ -137,7 +165,8 @@ struct cfg {
     u32a* err;
     u32a* owner;
     uint32_t order, thr_bits, max_threads;
-    uint32_t help_delay, enq_patience, deq_patience, remap;
+    uint32_t help_delay, enq_patience, deq_patience, remap, deq_wait;
+    u64a* stats;
     __host__ __device__ __forceinline__ uint32_t slots() const { return 2u << order; }
     __device__ __forceinline__ uint64_t cinc() const { return 1ULL << thr_bits; }
     __device__ __forceinline__ uint64_t null_tid() const { return (1ULL << thr_bits) - 1; }
@@ -169,6 +198,8 @@ __device__ __forceinline__ cfg load_cfg(const ring* q) {
     c.order = q->order; c.thr_bits = q->thr_bits; c.max_threads = q->max_threads;
     c.help_delay = q->help_delay; c.enq_patience = q->enq_patience; c.deq_patience = q->deq_patience;
     c.remap = q->remap;
+    c.deq_wait = q->deq_wait;
+    c.stats = q->stats;
     return c;
 }
 

@@ -56,6 +56,7 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
 // localTail holds ticket h.  The slot's owner entry names that record; the scan of
 // all records remains as the fallback when it no longer matches.
 __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j, uint32_t tid) {
+    GCQ_STAT(c, stat::FINALIZE);
     const uint64_t h_local = h_raw << 2;
     const uint32_t own = ld_rlx(&c.owner[j]);
     if (own != 0 && own <= c.max_threads) {
@@ -65,6 +66,7 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j
             return;
         }
     }
+    GCQ_STAT(c, stat::FINALIZE_SCAN);
     uint32_t i = (tid + 1 == c.max_threads) ? 0 : tid + 1;
     while (i != tid) {
         const uint64_t lt = ld_acq(&c.rec[i].localTail);
@@ -79,7 +81,7 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j
 // consume, gwf_ring.hpp:335-341
 __device__ __forceinline__ void consume(const cfg& c, uint64_t h_raw, uint32_t j, uint64_t e, uint32_t tid) {
     if (!entry::enq(e)) finalize_request(c, h_raw, j, tid);
-    fetch_or(&c.entry[j], entry::CONSUME_MASK);
+    fetch_or_acq(&c.entry[j], entry::CONSUME_MASK);   // acquire: the payload reads follow
 }
 
 // catchup, gwf_ring.hpp:348-371
@@ -104,20 +106,30 @@ __device__ inline void catchup(ring* q, const cfg& c, uint64_t tail_raw, uint64_
 // ------------------------------------------------------------------ fast path
 // try_enq, gwf_ring.hpp:382-414.  0 on success, else the ticket tried.
 __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
-    const uint64_t T = c.counter(warp_fetch_add(&q->Tail, c.cinc()));
+    GCQ_STAT(c, stat::TRY_ENQ);
+    const uint64_t T = c.counter(warp_ticket(&q->Tail, c.cinc()));
     const uint32_t tcyc = c.cycle_of(T);
     const uint32_t j = c.slot_of(T);
-    uint64_t E = ld_rlx(&c.entry[j]);
+    // In steady state the slot holds the previous cycle's consumed entry (Note
+    // untouched by any slow path, safe, index consumed): try the CAS against that
+    // value first.  A match means the enqueue conditions hold; a mismatch returns
+    // the slot's current value, exactly what the load of gwf_ring.hpp:394 would
+    // have read, so the code below continues from it.  Saves one L2 round trip.
+    uint64_t E = entry::pack(0xFF, tcyc - 1, true, true, BOT_C);
+    if (cas_upd_rel(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
+        if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+        return 0;
+    }
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
         const uint32_t ecyc = entry::cycle(E);
         const uint32_t eidx = entry::index(E);
         if (cycle_cmp(ecyc, tcyc) >= 0 || !entry::empty_index(eidx)) return T;
         if (!entry::safe(E)) {
             dekker_fence();
-            if (c.counter(ld_acq(&q->Head)) > T) return T;
+            if (c.counter(ld_rlx(&q->Head)) > T) return T;
         }
         const uint64_t nw = entry::pack(entry::note(E), tcyc, true, true, index);
-        if (!cas_upd(&c.entry[j], &E, nw)) continue;
+        if (!cas_upd_rel(&c.entry[j], &E, nw)) continue;   // release: publishes the payload
         if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
         return 0;
     }
@@ -128,10 +140,27 @@ __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
 // try_deq, gwf_ring.hpp:421-472.  0 when finished (*out = index, or BOT if the
 // queue is empty), else the ticket tried.
 __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_t tid) {
-    const uint64_t H = c.counter(warp_fetch_add(&q->Head, c.cinc()));
+    GCQ_STAT(c, stat::TRY_DEQ);
+    const uint64_t H = c.counter(warp_ticket(&q->Head, c.cinc()));
     const uint32_t hcyc = c.cycle_of(H);
     const uint32_t j = c.slot_of(H);
-    uint64_t E = ld_acq(&c.entry[j]);
+    uint64_t E = ld_rlx(&c.entry[j]);
+    // The slot of an earlier cycle with no index: the enqueuer holding this ticket
+    // may be about to fill it.  Marking it now would make that enqueuer retry with a
+    // new ticket, and this dequeuer too; re-reading it a few times first (bounded,
+    // so the operation stays wait-free) avoids that collision.
+    if (c.deq_wait && cycle_cmp(entry::cycle(E), hcyc) < 0 && entry::empty_index(entry::index(E))) {
+        uint32_t ns = 32;
+        for (uint32_t w = 0; w < c.deq_wait; ++w) {
+            __nanosleep(ns);
+            ns = ns < 1024 ? ns * 2 : ns;
+            E = ld_rlx(&c.entry[j]);
+            if (!(cycle_cmp(entry::cycle(E), hcyc) < 0 && entry::empty_index(entry::index(E)))) {
+                GCQ_STAT(c, stat::DEQ_WAITED);
+                break;
+            }
+        }
+    }
     uint32_t spin = 0;
     for (;; ++spin) {
         const uint32_t ecyc = entry::cycle(E);
@@ -146,10 +175,10 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
         const uint64_t nw = entry::empty_index(eidx)
                                 ? entry::pack(entry::note(E), hcyc, entry::safe(E), true, BOT)
                                 : entry::pack(entry::note(E), ecyc, false, entry::enq(E), eidx);
-        if (cas_upd(&c.entry[j], &E, nw)) break;
+        if (cas_upd_rlx(&c.entry[j], &E, nw)) break;
     }
     dekker_fence();
-    const uint64_t T = c.counter(ld_acq(&q->Tail));
+    const uint64_t T = c.counter(ld_rlx(&q->Tail));
     if (T <= H + 1) {
         catchup(q, c, T, H + 1);
         fetch_add(&q->Threshold, -1);
@@ -160,6 +189,7 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
         *out = BOT;
         return 0;
     }
+    GCQ_STAT(c, stat::DEQ_RETRY);
     return H;
 }
 
@@ -357,6 +387,7 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
         tail = try_enq(q, c, index);
         if (tail == 0) return;
     }
+    GCQ_STAT(c, stat::ENQ_SLOW);
     record* r = &c.rec[tid];
     const uint32_t seq = ld_rlx(&r->seq1);
     const uint64_t tail_local = tail << 2;
@@ -374,7 +405,7 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
 // Dequeue_wf, gwf_ring.hpp:1286-1356.  Returns the index or BOT when empty.
 __device__ inline uint32_t dequeue(ring* q, uint32_t tid) {
     const cfg c = load_cfg(q);
-    if (ld_acq(&q->Threshold) < 0) return BOT;
+    if (ld_rlx(&q->Threshold) < 0) return BOT;
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return BOT; }
     help_threads(q, c, tid);
     uint32_t out = BOT;
@@ -383,6 +414,7 @@ __device__ inline uint32_t dequeue(ring* q, uint32_t tid) {
         head = try_deq(q, c, &out, tid);
         if (head == 0) return out;
     }
+    GCQ_STAT(c, stat::DEQ_SLOW);
     record* r = &c.rec[tid];
     const uint32_t seq = ld_rlx(&r->seq1);
     const uint64_t head_local = head << 2;
@@ -454,6 +486,8 @@ __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
 #else
     h->remap = 0;
 #endif
+    h->deq_wait = 0;
+    h->stats = nullptr;
     __threadfence();
     // single thread: the slice covers the whole ring (no block sync needed
     // because gid 0 of a 1-thread group owns every element)
