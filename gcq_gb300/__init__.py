@@ -63,6 +63,11 @@ class BfsResult(C.Structure):
                 ("max_frontier", C.c_uint32), ("drops", C.c_uint32)]
 
 
+class RtResult(C.Structure):
+    _fields_ = [("gen_ms", C.c_double), ("trace_ms", C.c_double), ("total_ms", C.c_double),
+                ("primary_rays", C.c_uint64), ("total_rays", C.c_uint64), ("leftover", C.c_uint64)]
+
+
 class GcqError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = status
@@ -100,6 +105,7 @@ SIGNATURES = {
     "gcq_bfs_create": ([I32, P, P, C.c_int32, C.c_int64, U32, U32, C.POINTER(Knobs), C.POINTER(P)], I32),
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
+    "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
 }
 
 _LIB = None
@@ -313,6 +319,16 @@ class Bfs:
             self.close()
         except Exception:
             pass
+
+
+def rt_render(kind: str = "gwfq", scene: int = 0, width: int = 1280, height: int = 720, tiles_x: int = 8,
+              tiles_y: int = 8, threads_per_tile: int = 1024, max_bounces: int = 4, queue_log2: int = 15):
+    """Render one frame with the persistent per-tile ray tracer; returns (result, image HxWx3)."""
+    img = np.zeros((height, width, 3), dtype=np.float32)
+    r = RtResult()
+    _check(_lib().gcq_rt_render(KINDS[kind], scene, width, height, tiles_x, tiles_y, threads_per_tile,
+                                max_bounces, queue_log2, img.ctypes.data, C.byref(r)), "gcq_rt_render")
+    return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
 
 
 def roofline(reps: int = 3) -> dict:

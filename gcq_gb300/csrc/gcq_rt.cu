@@ -1,0 +1,472 @@
+// Persistent wavefront ray tracer with one queue per tile (concurrent_rt/rt_final.cpp):
+// k_generate writes every tile's primary rays and enqueues their pixel indices;
+// k_trace is one persistent launch in which each tile's threads dequeue rays, trace
+// them against the scene, accumulate colour with float atomicAdd and re-enqueue the
+// reflection ray until the tile's alive count reaches zero.
+//
+// This translation unit is compiled with --fmad=false: every a*b+c stays two
+// rounded operations, so with IEEE sqrtf and division the image equals a serial CPU
+// render that performs the same float operations in the same order.  A pixel's
+// contributions are added in bounce order (each bounce accumulates before it
+// re-enqueues the next), so the float sums are deterministic too.
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "gcq_internal.cuh"
+
+namespace {
+
+struct V3 { float x, y, z; };
+__host__ __device__ __forceinline__ V3 v3(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
+__host__ __device__ __forceinline__ V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ V3 scale(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ V3 mulv(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ V3 normalize(V3 v) {
+    const float d = sqrtf(dot3(v, v));
+    return d > 0.f ? scale(v, 1.f / d) : v;
+}
+__host__ __device__ __forceinline__ V3 reflect3(V3 v, V3 n) { return sub(v, scale(n, 2.f * dot3(v, n))); }
+__host__ __device__ __forceinline__ V3 clamp01(V3 c) {
+    return v3(fminf(fmaxf(c.x, 0.f), 1.f), fminf(fmaxf(c.y, 0.f), 1.f), fminf(fmaxf(c.z, 0.f), 1.f));
+}
+
+// rt_final.cpp:350-366
+struct Sphere { V3 c; float r; V3 albedo; float refl; };
+struct Plane { V3 n; float d; V3 albedo; float refl; };
+struct Ray { V3 o, d; int px, py, depth; V3 atten; };   // 48 bytes, as the reference's Ray
+struct Hit { float t; V3 n, p, albedo; float refl; bool did_hit; };
+
+// intersect_sphere / intersect_plane / trace_scene, rt_final.cpp:371-419
+__device__ __forceinline__ Hit hit_sphere(const Ray& ray, const Sphere& s) {
+    Hit h; h.did_hit = false; h.t = 1e30f;
+    const V3 oc = sub(ray.o, s.c);
+    const float b = dot3(oc, ray.d);
+    const float c = dot3(oc, oc) - s.r * s.r;
+    const float disc = b * b - c;
+    if (disc >= 0.f) {
+        const float t = -b - sqrtf(disc);
+        if (t > 1e-4f) {
+            h.t = t; h.did_hit = true;
+            h.p = add(ray.o, scale(ray.d, t));
+            h.n = normalize(sub(h.p, s.c));
+            h.albedo = s.albedo;
+            h.refl = s.refl;
+        }
+    }
+    return h;
+}
+__device__ __forceinline__ Hit hit_plane(const Ray& ray, const Plane& pl) {
+    Hit h; h.did_hit = false; h.t = 1e30f;
+    const float denom = dot3(pl.n, ray.d);
+    if (fabsf(denom) > 1e-5f) {
+        const float t = -(dot3(pl.n, ray.o) + pl.d) / denom;
+        if (t > 1e-4f) {
+            h.t = t; h.did_hit = true;
+            h.p = add(ray.o, scale(ray.d, t));
+            h.n = pl.n;
+            h.albedo = pl.albedo;
+            h.refl = pl.refl;
+        }
+    }
+    return h;
+}
+__device__ __forceinline__ Hit trace_scene(const Ray& ray, const Sphere* sph, int ns, const Plane* pln, int np) {
+    Hit best; best.did_hit = false; best.t = 1e30f;
+    for (int i = 0; i < ns; i++) {
+        const Hit h = hit_sphere(ray, sph[i]);
+        if (h.did_hit && h.t < best.t) best = h;
+    }
+    for (int i = 0; i < np; i++) {
+        const Hit h = hit_plane(ray, pln[i]);
+        if (h.did_hit && h.t < best.t) best = h;
+    }
+    return best;
+}
+
+__device__ __forceinline__ void accum_pixel(float* img, int w, int x, int y, V3 c) {
+    float* p = img + 3 * (size_t)(y * w + x);
+    atomicAdd(p + 0, c.x);
+    atomicAdd(p + 1, c.y);
+    atomicAdd(p + 2, c.z);
+}
+
+// ---------------------------------------------------------------- per-tile queues
+// Raw index rings as the reference uses them (rt_final.cpp:53-298): G-WFQ wf_t,
+// G-LFQ fq_ring_t, SFQ with the index shifted by one (0 is reserved).
+struct tile_queues {
+    int kind;
+    void* rings;          // array of gwf::ring / glf::ring / sfq::queue, one per tile
+    size_t stride;        // bytes between consecutive ring headers
+};
+
+template <int K> struct rtq;
+template <> struct rtq<GCQ_GWFQ> {
+    using R = gcq::gwf::ring;
+    __device__ static bool enq(R* q, uint32_t idx, uint32_t tid) { gcq::gwf::enqueue(q, idx, tid); return true; }
+    __device__ static bool deq(R* q, uint32_t* out, uint32_t tid) {
+        *out = gcq::gwf::dequeue(q, tid);
+        return *out != gcq::gwf::BOT;
+    }
+};
+template <> struct rtq<GCQ_GLFQ> {
+    using R = gcq::glf::ring;
+    __device__ static bool enq(R* q, uint32_t idx, uint32_t) { return gcq::glf::enqueue(q, idx); }
+    __device__ static bool deq(R* q, uint32_t* out, uint32_t) {
+        *out = gcq::glf::dequeue(q);
+        return *out != gcq::glf::BOT;
+    }
+};
+template <> struct rtq<GCQ_SFQ> {
+    using R = gcq::sfq::queue;
+    __device__ static bool enq(R* q, uint32_t idx, uint32_t) { return gcq::sfq::enqueue_blocking(q, idx + 1u) == SFQ_SUCCESS; }
+    __device__ static bool deq(R* q, uint32_t* out, uint32_t) {
+        uint32_t item = 0;
+        if (gcq::sfq::dequeue_nb(q, &item) != SFQ_SUCCESS) return false;
+        *out = item - 1u;
+        return true;
+    }
+};
+
+struct rt_params {
+    int img_w, img_h, tiles_x, tile_w, tile_h, threads_per_tile, max_depth;
+    V3 cam_o, cam_f, cam_r, cam_u;
+    uint64_t timeout_ns;
+};
+
+// k_generate, rt_final.cpp:435-511
+template <int K>
+__global__ void k_generate(char* rings, size_t stride, Ray* __restrict__ rays, rt_params P,
+                           unsigned long long* __restrict__ alive) {
+    const int tile = (int)blockIdx.y;
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (tid >= P.threads_per_tile) return;
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
+    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
+    const int tw = min(P.tile_w, P.img_w - x0), th = min(P.tile_h, P.img_h - y0);
+    const int tile_pixels = tw * th;
+    const float aspect = (float)P.img_w / (float)P.img_h;
+    int enqueued = 0;
+    for (int i = tid; i < tile_pixels; i += P.threads_per_tile) {
+        const int lx = i % tw, ly = i / tw;
+        const int px = x0 + lx, py = y0 + ly;
+        const float u = ((px + 0.5f) / P.img_w - 0.5f) * 2.f * aspect;
+        const float v = -((py + 0.5f) / P.img_h - 0.5f) * 2.f;
+        Ray r;
+        r.o = P.cam_o;
+        r.d = normalize(add(add(P.cam_f, scale(P.cam_r, u)), scale(P.cam_u, v)));
+        r.px = px; r.py = py;
+        r.depth = 0;
+        r.atten = v3(1.f, 1.f, 1.f);
+        rays[py * P.img_w + px] = r;
+        // the queue's release CAS publishes the ray written above
+        if (rtq<K>::enq(q, (uint32_t)i, (uint32_t)tid)) ++enqueued;
+    }
+    if (enqueued > 0) atomicAdd(&alive[tile], (unsigned long long)enqueued);
+}
+
+// k_trace, rt_final.cpp:516-645.  The wait for in-flight rays is bounded: with no
+// progress for timeout_ns the thread records ERR_TIMEOUT and leaves.
+template <int K>
+__global__ void k_trace(char* rings, size_t stride, const Sphere* __restrict__ sph, int ns,
+                        const Plane* __restrict__ pln, int np, Ray* __restrict__ rays, float* __restrict__ img,
+                        rt_params P, unsigned long long* __restrict__ alive, unsigned long long* __restrict__ traced,
+                        gcq::u32a* err) {
+    const int tile = (int)blockIdx.y;
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (tid >= P.threads_per_tile) return;
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
+    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
+    const int tw = min(P.tile_w, P.img_w - x0);
+    const V3 light_dir = normalize(v3(-0.5f, 1.f, 0.2f));
+    const V3 ambient = v3(0.05f, 0.05f, 0.05f);
+    unsigned long long local_traced = 0;
+    gcq::backoff bo;
+    uint64_t last_progress = gcq::globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+        if (gcq::ld_rlx((const gcq::u64a*)&alive[tile]) == 0) break;
+        uint32_t local_idx;
+        if (!rtq<K>::deq(q, &local_idx, (uint32_t)tid)) {
+            if ((it & 63) == 0 && gcq::globaltimer_ns() - last_progress > P.timeout_ns) {
+                gcq::raise_error(err, gcq::ERR_TIMEOUT);
+                break;
+            }
+            bo.pause(1024);
+            continue;
+        }
+        bo = gcq::backoff();
+        last_progress = gcq::globaltimer_ns();
+        const int lx = (int)local_idx % tw, ly = (int)local_idx / tw;
+        const int gidx = (y0 + ly) * P.img_w + (x0 + lx);
+        const Ray r = rays[gidx];
+        const Hit hit = trace_scene(r, sph, ns, pln, np);
+        if (hit.did_hit) {
+            const float NdotL = fmaxf(0.f, dot3(hit.n, light_dir));
+            const V3 direct = add(ambient, scale(hit.albedo, NdotL));
+            const V3 contrib = mulv(direct, r.atten);
+            if (hit.refl > 0.f && r.depth < P.max_depth) {
+                const V3 non_refl = clamp01(scale(contrib, 1.f - hit.refl));
+                if (non_refl.x > 0.f || non_refl.y > 0.f || non_refl.z > 0.f)
+                    accum_pixel(img, P.img_w, r.px, r.py, non_refl);
+                Ray refl;
+                refl.o = add(hit.p, scale(hit.n, 1e-4f));
+                refl.d = normalize(reflect3(r.d, hit.n));
+                refl.px = r.px; refl.py = r.py;
+                refl.depth = r.depth + 1;
+                refl.atten = scale(mulv(r.atten, hit.albedo), hit.refl);
+                rays[gidx] = refl;
+                if (!rtq<K>::enq(q, local_idx, (uint32_t)tid)) atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+            } else {
+                accum_pixel(img, P.img_w, r.px, r.py, clamp01(contrib));
+                atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+            }
+        } else {
+            const float t = 0.5f * (r.d.y + 1.f);
+            const V3 sky = add(scale(v3(1.f, 1.f, 1.f), 1.f - t), scale(v3(0.5f, 0.7f, 1.f), t));
+            accum_pixel(img, P.img_w, r.px, r.py, clamp01(mulv(sky, r.atten)));
+            atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+        }
+        ++local_traced;
+    }
+    if (local_traced > 0) atomicAdd(&traced[tile], local_traced);
+}
+
+// Per-tile ring initialisation (the reference's k_init_queue, rt_final.cpp:84-139).
+__global__ void k_init_tiles_gwf(char* rings, size_t stride, int tiles) {
+    for (int t = blockIdx.y; t < tiles; t += gridDim.y)
+        gcq::gwf::init_slice((gcq::gwf::ring*)(rings + (size_t)t * stride), false,
+                             (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+}
+__global__ void k_init_tiles_glf(char* rings, size_t stride, int tiles) {
+    for (int t = blockIdx.y; t < tiles; t += gridDim.y)
+        gcq::glf::init_slice((gcq::glf::ring*)(rings + (size_t)t * stride), false,
+                             (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+}
+__global__ void k_init_tiles_sfq(char* rings, size_t stride, int tiles) {
+    for (int t = blockIdx.y; t < tiles; t += gridDim.y)
+        gcq::sfq::init_slice((gcq::sfq::queue*)(rings + (size_t)t * stride),
+                             (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+}
+
+// Scenes of rt_final.cpp:650-684 and cameras of :849-859.
+void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, rt_params& P) {
+    if (scene == 0) {
+        pln.push_back({v3(0, 1, 0), 1.f, v3(0.75f, 0.75f, 0.75f), 0.05f});
+        const int gx = 10, gz = 10;
+        const float sp = 0.55f, rad = 0.22f, base_y = 0.25f;
+        for (int iz = 0; iz < gz; iz++)
+            for (int ix = 0; ix < gx; ix++) {
+                const float x = (ix - (gx - 1) * 0.5f) * sp;
+                const float z = -2.f - iz * sp;
+                const int m = (ix + iz * 7) % 7;
+                const float r = (m == 0) ? 0.9f : (m == 1) ? 0.6f : (m == 2) ? 0.3f : (m == 3) ? 0.1f : 0.f;
+                const V3 a = (m == 0) ? v3(.9f, .9f, .9f) : (m == 1) ? v3(.9f, .5f, .2f)
+                           : (m == 2) ? v3(.2f, .8f, .9f) : (m == 3) ? v3(.7f, .2f, .8f)
+                           : (m == 4) ? v3(.2f, .9f, .3f) : (m == 5) ? v3(.9f, .2f, .2f) : v3(.8f, .8f, .3f);
+                sph.push_back({v3(x, base_y, z), rad, a, r});
+            }
+        sph.push_back({v3(-1.2f, 0.6f, -3.5f), 0.6f, v3(.9f, .3f, .3f), 0.7f});
+        sph.push_back({v3(1.4f, 0.9f, -4.2f), 0.9f, v3(.3f, .9f, .4f), 0.2f});
+        sph.push_back({v3(0.0f, 1.3f, -5.5f), 1.3f, v3(.4f, .6f, .95f), 0.0f});
+        P.cam_o = v3(0, 0.3f, 0.5f);
+        P.cam_f = normalize(v3(0, -0.2f, -1.f));
+    } else {
+        sph.push_back({v3(-0.6f, 0.5f, -2.5f), 0.5f, v3(.9f, .3f, .3f), 0.85f});
+        sph.push_back({v3(0.6f, 0.6f, -2.8f), 0.6f, v3(.95f, .95f, .95f), 0.95f});
+        pln.push_back({v3(0, 1, 0), 1.f, v3(.9f, .9f, .9f), 0.3f});
+        pln.push_back({v3(0, 0, 1), 5.f, v3(.6f, .65f, .8f), 0.7f});
+        pln.push_back({v3(1, 0, 0), 2.f, v3(.8f, .2f, .2f), 0.6f});
+        pln.push_back({v3(-1, 0, 0), 2.f, v3(.2f, .8f, .3f), 0.6f});
+        pln.push_back({v3(0, -1, 0), 2.5f, v3(.95f, .95f, .95f), 0.2f});
+        P.cam_o = v3(0, 0.5f, 1.5f);
+        P.cam_f = normalize(v3(0, -0.1f, -1.f));
+    }
+    P.cam_r = normalize(v3(1, 0, 0));
+    P.cam_u = normalize(v3(0, 1, 0));
+}
+
+}  // namespace
+
+extern "C" {
+
+// Render one frame (rt_final.cpp:705-1018).  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ
+// (YMC's per-tile pool runs dry under the persistent loop's failed dequeues and
+// drops rays, as the reference's would; it is not offered here).  image receives
+// width*height RGB float pixels (may be NULL).
+int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
+                  int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out) {
+    if (!out || width <= 0 || height <= 0 || tiles_x <= 0 || tiles_y <= 0 || threads_per_tile <= 0 ||
+        max_bounces < 0 || (scene != 0 && scene != 1) || queue_log2 < 4 || queue_log2 > 24)
+        return GCQ_EINVAL;
+    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
+    memset(out, 0, sizeof(*out));
+    const int tiles = tiles_x * tiles_y;
+    rt_params P;
+    memset(&P, 0, sizeof P);
+    P.img_w = width; P.img_h = height; P.tiles_x = tiles_x;
+    P.tile_w = (width + tiles_x - 1) / tiles_x;
+    P.tile_h = (height + tiles_y - 1) / tiles_y;
+    P.threads_per_tile = threads_per_tile;
+    P.max_depth = max_bounces;
+    P.timeout_ns = 5000000000ull;
+    const uint64_t tile_px = (uint64_t)P.tile_w * P.tile_h;
+    const uint64_t n = 1ull << queue_log2;
+    if (tile_px > n) return GCQ_ECAPACITY;   // a tile's rays must fit its queue
+    std::vector<Sphere> sph;
+    std::vector<Plane> pln;
+    build_scene(scene, sph, pln, P);
+
+    // ---- per-tile queues in one allocation
+    size_t stride = 0, per_tile = 0;
+    if (kind == GCQ_GWFQ) {
+        if ((uint64_t)threads_per_tile > n) return GCQ_EUNSUPPORTED;
+        int bits = 5;
+        while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
+        stride = sizeof(gcq::gwf::ring);
+        // entries (256-B aligned), records (128 B each), help countdowns (8 B), owners
+        per_tile = ((2 * n * 8 + 255) / 256 * 256) + (size_t)threads_per_tile * (sizeof(gcq::gwf::record) + 8) +
+                   2 * n * 4;
+        (void)bits;
+    } else if (kind == GCQ_GLFQ) {
+        stride = sizeof(gcq::glf::ring);
+        per_tile = 2 * n * 8;
+    } else {
+        const uint64_t max_id = 2ull * ((0xFFFFFFFFull / n) + 1);
+        if (max_id < 2ull * ((uint64_t)threads_per_tile + 1)) return GCQ_EUNSUPPORTED;
+        stride = sizeof(gcq::sfq::queue);
+        per_tile = n * 8;
+    }
+    auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t hdr_bytes = a256(stride * tiles);
+    const size_t tile_bytes = a256(per_tile);
+    const size_t q_bytes = hdr_bytes + tile_bytes * tiles + 256;
+    const size_t ray_bytes = (size_t)width * height * sizeof(Ray);
+    const size_t img_bytes = (size_t)width * height * 3 * sizeof(float);
+    char* dq = nullptr;
+    Ray* d_rays = nullptr;
+    float* d_img = nullptr;
+    unsigned long long* d_cnt = nullptr;   // alive[tiles], traced[tiles]
+    Sphere* d_sph = nullptr;
+    Plane* d_pln = nullptr;
+    auto cleanup = [&]() { cudaFree(dq); cudaFree(d_rays); cudaFree(d_img); cudaFree(d_cnt); cudaFree(d_sph); cudaFree(d_pln); };
+    if (cudaMalloc(&dq, q_bytes) != cudaSuccess || cudaMalloc(&d_rays, ray_bytes) != cudaSuccess ||
+        cudaMalloc(&d_img, img_bytes) != cudaSuccess || cudaMalloc(&d_cnt, 2 * tiles * 8) != cudaSuccess ||
+        cudaMalloc(&d_sph, std::max<size_t>(1, sph.size()) * sizeof(Sphere)) != cudaSuccess ||
+        cudaMalloc(&d_pln, std::max<size_t>(1, pln.size()) * sizeof(Plane)) != cudaSuccess) {
+        cleanup();
+        return GCQ_ENOMEM;
+    }
+    gcq::u32a* d_err = (gcq::u32a*)(dq + hdr_bytes + tile_bytes * tiles);
+    {
+        std::vector<char> hh(hdr_bytes, 0);
+        for (int t = 0; t < tiles; ++t) {
+            char* tb = dq + hdr_bytes + tile_bytes * t;
+            if (kind == GCQ_GWFQ) {
+                int bits = 5;
+                while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
+                gcq::gwf::ring r;
+                memset(&r, 0, sizeof r);
+                r.Entry = (gcq::u64a*)tb;
+                r.Record = (gcq::gwf::record*)(tb + a256(2 * n * 8));
+                r.Help = (gcq::gwf::helper_state*)((char*)r.Record + (size_t)threads_per_tile * sizeof(gcq::gwf::record));
+                r.Owner = (gcq::u32a*)((char*)r.Help + (size_t)threads_per_tile * 8);
+                r.err = d_err;
+                r.order = queue_log2;
+                r.thr_bits = (uint32_t)bits;
+                r.max_threads = (uint32_t)threads_per_tile;
+                r.help_delay = WF_HELP_DELAY;
+                r.enq_patience = WF_ENQ_PATIENCE;
+                r.deq_patience = WF_DEQ_PATIENCE;
+                r.remap = 0;
+                r.deq_wait = 0;
+                r.stats = nullptr;
+                memcpy(&hh[t * stride], &r, sizeof r);
+            } else if (kind == GCQ_GLFQ) {
+                gcq::glf::ring r;
+                memset(&r, 0, sizeof r);
+                r.Entry = (gcq::u64a*)tb;
+                r.err = d_err;
+                r.order = queue_log2;
+                r.line_log2 = 3;   // the reference's 64-byte remap (glf_queue.hpp:50-51)
+                r.deq_wait = 0;
+                memcpy(&hh[t * stride], &r, sizeof r);
+            } else {
+                gcq::sfq::queue r;
+                memset(&r, 0, sizeof r);
+                r.slot = (gcq::u64a*)tb;
+                r.err = d_err;
+                r.log2_len = queue_log2;
+                r.max_id = (uint32_t)(2ull * ((0xFFFFFFFFull / n) + 1));
+                r.timeout_ns = P.timeout_ns;
+                r.nprocs = (uint32_t)threads_per_tile;
+                memcpy(&hh[t * stride], &r, sizeof r);
+            }
+        }
+        GCQ_CUDA(cudaMemcpy(dq, hh.data(), hdr_bytes, cudaMemcpyHostToDevice));
+    }
+    GCQ_CUDA(cudaMemset(d_err, 0, 4));
+    GCQ_CUDA(cudaMemset(d_img, 0, img_bytes));
+    GCQ_CUDA(cudaMemset(d_cnt, 0, 2 * tiles * 8));
+    if (!sph.empty()) GCQ_CUDA(cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(Sphere), cudaMemcpyHostToDevice));
+    if (!pln.empty()) GCQ_CUDA(cudaMemcpy(d_pln, pln.data(), pln.size() * sizeof(Plane), cudaMemcpyHostToDevice));
+    {
+        const dim3 ig((unsigned)std::min<uint64_t>(64, (2 * n + 255) / 256), (unsigned)std::min(tiles, 1024));
+        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(dq, stride, tiles);
+        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(dq, stride, tiles);
+        else k_init_tiles_sfq<<<ig, 256>>>(dq, stride, tiles);
+        GCQ_CUDA(cudaGetLastError());
+        GCQ_CUDA(cudaDeviceSynchronize());
+    }
+    const int TPB = 256;
+    const dim3 grid((unsigned)((threads_per_tile + TPB - 1) / TPB), (unsigned)tiles);
+    cudaEvent_t e0, e1, e2;
+    cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&e2);
+    unsigned long long* d_alive = d_cnt;
+    unsigned long long* d_traced = d_cnt + tiles;
+    const int ns = (int)sph.size(), np = (int)pln.size();
+    cudaEventRecord(e0);
+    if (kind == GCQ_GWFQ) k_generate<GCQ_GWFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
+    else if (kind == GCQ_GLFQ) k_generate<GCQ_GLFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
+    else k_generate<GCQ_SFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
+    cudaEventRecord(e1);
+    if (kind == GCQ_GWFQ)
+        k_trace<GCQ_GWFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
+    else if (kind == GCQ_GLFQ)
+        k_trace<GCQ_GLFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
+    else
+        k_trace<GCQ_SFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
+    cudaEventRecord(e2);
+    cudaError_t ke = cudaEventSynchronize(e2);
+    if (ke == cudaSuccess) ke = cudaGetLastError();
+    if (ke != cudaSuccess) {
+        cleanup();
+        return gcqi::cuda_fail(ke, "rt kernels", __FILE__, __LINE__);
+    }
+    float gen_ms = 0, trace_ms = 0;
+    cudaEventElapsedTime(&gen_ms, e0, e1);
+    cudaEventElapsedTime(&trace_ms, e1, e2);
+    cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+    std::vector<unsigned long long> cnt(2 * tiles);
+    GCQ_CUDA(cudaMemcpy(cnt.data(), d_cnt, 2 * tiles * 8, cudaMemcpyDeviceToHost));
+    uint32_t err = 0;
+    GCQ_CUDA(cudaMemcpy(&err, d_err, 4, cudaMemcpyDeviceToHost));
+    uint64_t leftover = 0, traced = 0;
+    for (int t = 0; t < tiles; ++t) { leftover += cnt[t]; traced += cnt[tiles + t]; }
+    out->gen_ms = gen_ms;
+    out->trace_ms = trace_ms;
+    out->total_ms = gen_ms + trace_ms;
+    out->primary_rays = (uint64_t)width * height;
+    out->total_rays = traced;
+    out->leftover = leftover;
+    if (image) GCQ_CUDA(cudaMemcpy(image, d_img, img_bytes, cudaMemcpyDeviceToHost));
+    cleanup();
+    if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
+    if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
+    return leftover ? GCQ_EDEVICE : GCQ_OK;
+}
+
+}  // extern "C"

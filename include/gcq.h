@@ -251,6 +251,25 @@ int gcq_bfs_destroy(gcq_bfs_ctx* c);
 int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int32_t* host_levels,
                 gcq_bfs_result* out);
 
+/* ------------------------------------------------------------ ray tracer ----
+ * Persistent per-tile ray tracer (concurrent_rt/rt_final.cpp). */
+typedef struct gcq_rt_result {
+    double gen_ms;          /* k_generate */
+    double trace_ms;        /* k_trace: every bounce in one launch */
+    double total_ms;
+    uint64_t primary_rays;
+    uint64_t total_rays;    /* rays traced, bounces included */
+    uint64_t leftover;      /* rays still alive after the trace (must be 0) */
+} gcq_rt_result;
+
+/* Render one frame of the reference scene `scene` (0 spheres, 1 Cornell-style box;
+ * rt_final.cpp:650-684, cameras :849-859) at width x height in tiles_x x tiles_y
+ * tiles, threads_per_tile workers and one queue of 2^queue_log2 per tile, up to
+ * max_bounces reflections.  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ.  image (may be
+ * NULL) receives width*height RGB floats.  Replaces rt_final.cpp:705-1018. */
+int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
+                  int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out);
+
 /* ------------------------------------------------------------- roofline ----
  * The atomic roofline of this GPU, measured by a microbenchmark in the same
  * process (the reference reports raw Mops/s only).  Rates are operations per

@@ -72,8 +72,7 @@ def lib():
 
 _EXTRA = [
     ("oracle_bfs", [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int32),
-    ("oracle_rt_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                          C.c_void_p], C.c_int),
+    ("oracle_rt_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p], C.c_int64),
 ]
 
 
