@@ -102,6 +102,8 @@ SIGNATURES = {
     "gcq_graph_grid": ([U32, U32, C.c_double, C.c_double, U64, C.POINTER(P), C.POINTER(P),
                         C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
     "gcq_free": ([P], None),
+    "gcq_graph_rmat": ([U32, U32, C.c_double, C.c_double, C.c_double, U64, C.POINTER(P), C.POINTER(P),
+                        C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
     "gcq_bfs_create": ([I32, P, P, C.c_int32, C.c_int64, U32, U32, C.POINTER(Knobs), C.POINTER(P)], I32),
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
@@ -271,6 +273,20 @@ def graph_grid(rows: int, cols: int, keep_p: float = 0.6, diag_p: float = 0.01, 
     V, E = C.c_int32(), C.c_int64()
     _check(_lib().gcq_graph_grid(rows, cols, keep_p, diag_p, seed, C.byref(po), C.byref(pi),
                                  C.byref(V), C.byref(E)), "gcq_graph_grid")
+    off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int32)), shape=(V.value + 1,)).copy()
+    idx = np.ctypeslib.as_array(C.cast(pi, C.POINTER(C.c_int32)), shape=(max(E.value, 1),))[: E.value].copy()
+    _lib().gcq_free(po)
+    _lib().gcq_free(pi)
+    return off, idx
+
+
+def graph_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+               seed: int = 1):
+    """Seeded R-MAT graph as CSR int32 numpy arrays (gcq_graph_rmat)."""
+    po, pi = P(), P()
+    V, E = C.c_int32(), C.c_int64()
+    _check(_lib().gcq_graph_rmat(scale, edge_factor, a, b, c, seed, C.byref(po), C.byref(pi),
+                                 C.byref(V), C.byref(E)), "gcq_graph_rmat")
     off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int32)), shape=(V.value + 1,)).copy()
     idx = np.ctypeslib.as_array(C.cast(pi, C.POINTER(C.c_int32)), shape=(max(E.value, 1),))[: E.value].copy()
     _lib().gcq_free(po)

@@ -4,8 +4,10 @@
 // cooperative launch for the whole traversal, levels separated by a bounded grid
 // barrier).  Also the seeded grid-graph generator of the benchmark graphs.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "gcq_internal.cuh"
@@ -502,6 +504,85 @@ int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
     if (err & GCQ_ERR_POOL) return GCQ_ECAPACITY;
+    return GCQ_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ RMAT graphs
+extern "C" {
+
+// Seeded R-MAT graph (Chakrabarti, Zhan & Faloutsos, SDM 2004): 2^scale vertices,
+// edge_factor * 2^scale generated edges, each placed by descending `scale` levels of
+// the adjacency matrix with quadrant probabilities a, b, c, 1-a-b-c.  Self loops and
+// duplicates are removed; the result is undirected CSR with ascending neighbours.
+// Built in parallel on the host cores: edges are generated per thread from the edge
+// index (so the graph does not depend on the thread count), scattered into CSR, and
+// every adjacency list is sorted and deduplicated.  The reference has no generator
+// (it loads .mtx/SNAP files, bfs_bench.cpp:202-243).
+int gcq_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                   int32_t** offsets, int32_t** indices, int32_t* V_out, int64_t* E_out) {
+    if (!offsets || !indices || !V_out || !E_out || scale < 1 || scale > 30 || edge_factor == 0) return GCQ_EINVAL;
+    if (a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return GCQ_EINVAL;
+    const uint64_t V = 1ull << scale;
+    const uint64_t M = (uint64_t)edge_factor * V;
+    const double ab = a + b, abc = a + b + c;
+    const unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    auto par = [&](uint64_t n, auto&& body) {
+        std::vector<std::thread> ts;
+        for (unsigned t = 0; t < nth; ++t)
+            ts.emplace_back([&, t]() { for (uint64_t i = n * t / nth; i < n * (t + 1) / nth; ++i) body(i); });
+        for (auto& th : ts) th.join();
+    };
+    std::vector<uint32_t> eu(M), ev(M);
+    par(M, [&](uint64_t e) {
+        uint64_t u = 0, v = 0;
+        uint64_t h = mix(seed * 0xD1B54A32D192ED03ull + e);
+        for (uint32_t l = 0; l < scale; ++l) {
+            h = mix(h + 0x9E3779B97F4A7C15ull);
+            const double r = unit(h);
+            const uint64_t bit = 1ull << (scale - 1 - l);
+            if (r < a) {}
+            else if (r < ab) v |= bit;
+            else if (r < abc) u |= bit;
+            else { u |= bit; v |= bit; }
+        }
+        eu[e] = (uint32_t)u;
+        ev[e] = (uint32_t)v;
+    });
+    std::vector<std::atomic<int32_t>> deg(V);
+    par(V, [&](uint64_t v) { deg[v].store(0, std::memory_order_relaxed); });
+    par(M, [&](uint64_t e) {
+        if (eu[e] == ev[e]) return;
+        deg[eu[e]].fetch_add(1, std::memory_order_relaxed);
+        deg[ev[e]].fetch_add(1, std::memory_order_relaxed);
+    });
+    std::vector<int64_t> start(V + 1, 0);
+    for (uint64_t v = 0; v < V; ++v) start[v + 1] = start[v] + deg[v].load(std::memory_order_relaxed);
+    std::vector<int32_t> adj((size_t)std::max<int64_t>(start[V], 1));
+    std::vector<std::atomic<int64_t>> cur(V);
+    par(V, [&](uint64_t v) { cur[v].store(start[v], std::memory_order_relaxed); });
+    par(M, [&](uint64_t e) {
+        if (eu[e] == ev[e]) return;
+        adj[cur[eu[e]].fetch_add(1, std::memory_order_relaxed)] = (int32_t)ev[e];
+        adj[cur[ev[e]].fetch_add(1, std::memory_order_relaxed)] = (int32_t)eu[e];
+    });
+    std::vector<int32_t> ndeg(V);
+    par(V, [&](uint64_t v) {
+        int32_t* b0 = adj.data() + start[v];
+        int32_t* e0 = adj.data() + start[v + 1];
+        std::sort(b0, e0);
+        ndeg[v] = (int32_t)(std::unique(b0, e0) - b0);
+    });
+    int32_t* off = (int32_t*)malloc((V + 1) * sizeof(int32_t));
+    if (!off) return GCQ_ENOMEM;
+    off[0] = 0;
+    for (uint64_t v = 0; v < V; ++v) off[v + 1] = off[v] + ndeg[v];
+    const int64_t E = off[V];
+    int32_t* idx = (int32_t*)malloc((size_t)std::max<int64_t>(E, 1) * sizeof(int32_t));
+    if (!idx) { free(off); return GCQ_ENOMEM; }
+    par(V, [&](uint64_t v) { std::copy(adj.data() + start[v], adj.data() + start[v] + ndeg[v], idx + off[v]); });
+    *offsets = off; *indices = idx; *V_out = (int32_t)V; *E_out = E;
     return GCQ_OK;
 }
 

@@ -234,6 +234,13 @@ int gcq_graph_grid(uint32_t rows, uint32_t cols, double keep_p, double diag_p, u
                    int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
 void gcq_free(void* p);
 
+/* Seeded R-MAT graph with 2^scale vertices and edge_factor * 2^scale generated
+ * edges (quadrant probabilities a, b, c, 1-a-b-c), self loops and duplicates
+ * removed, undirected CSR.  Arrays as for gcq_graph_grid.  No counterpart in the
+ * reference, which reads graph files (bfs_bench.cpp:202-243). */
+int gcq_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                   int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
+
 /* Upload the CSR and create the two frontier queues of `kind` for `threads`
  * worker threads (a multiple of 32) with capacity 2^capacity_log2 (0 = the
  * smallest power of two >= V, at least 2^15, within the queue's envelope).
