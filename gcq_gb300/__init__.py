@@ -68,6 +68,26 @@ class RtResult(C.Structure):
                 ("primary_rays", C.c_uint64), ("total_rays", C.c_uint64), ("leftover", C.c_uint64)]
 
 
+class ServeCfg(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("timeout_ns", C.c_uint64), ("max_slots", C.c_uint32),
+                ("threads", C.c_uint32), ("work_log2", C.c_uint32), ("_pad", C.c_uint32),
+                ("run_limit_ns", C.c_uint64), ("work_knobs", Knobs)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("items", C.c_uint64), ("stale", C.c_uint64),
+                ("edges", C.c_uint64), ("sweeps", C.c_uint64), ("completed", C.c_uint32),
+                ("error_word", C.c_uint32), ("released", C.c_uint32), ("inflight", C.c_uint32),
+                ("reserved", C.c_uint64), ("work_tail", C.c_uint64 * 2), ("work_head", C.c_uint64 * 2),
+                ("work_threshold", C.c_int32 * 2)]
+
+
+# gcq_serve_req / gcq_serve_res (include/gcq.h)
+SERVE_REQ_DTYPE = np.dtype([("graph", "<i4"), ("src", "<i4"), ("arrival_ns", "<u8")])
+SERVE_RES_DTYPE = np.dtype([("admit_ns", "<u8"), ("done_ns", "<u8"), ("finish_ns", "<u8"),
+                            ("checksum", "<u8"), ("reached", "<u4"), ("max_level", "<i4")])
+
+
 class GcqError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = status
@@ -108,6 +128,11 @@ SIGNATURES = {
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
     "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
+    "gcq_serve_default_cfg": ([C.POINTER(ServeCfg)], None),
+    "gcq_serve_create": ([I32, P, P, P, P, C.POINTER(ServeCfg), C.POINTER(P)], I32),
+    "gcq_serve_destroy": ([P], I32),
+    "gcq_serve_info": ([P, I32, C.POINTER(U32), C.POINTER(U32), C.POINTER(U64)], I32),
+    "gcq_serve_run": ([P, P, U32, P, C.POINTER(ServeStats)], I32),
 }
 
 _LIB = None
@@ -335,6 +360,91 @@ class Bfs:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Persistent BFS server over resident CSR graphs (gcq_serve_create / gcq_serve_run).
+
+    graphs: a list of (offsets, indices) int32 CSR pairs.  run() takes a structured
+    array of SERVE_REQ_DTYPE sorted by arrival_ns and returns (SERVE_RES_DTYPE
+    array, stats dict)."""
+
+    def __init__(self, graphs, budget_bytes: int | None = None, max_slots: int = 0, threads: int = 0,
+                 work_log2: int = 0, timeout_s: float = 0.0, run_limit_s: float = 0.0, **work_knobs):
+        self.graphs = [(np.ascontiguousarray(o, dtype=np.int32), np.ascontiguousarray(i, dtype=np.int32))
+                       for o, i in graphs]
+        n = len(self.graphs)
+        offs = (C.c_void_p * n)(*[o.ctypes.data for o, _ in self.graphs])
+        idxs = (C.c_void_p * n)(*[i.ctypes.data for _, i in self.graphs])
+        self.V = np.array([len(o) - 1 for o, _ in self.graphs], dtype=np.int32)
+        E = np.array([len(i) for _, i in self.graphs], dtype=np.int64)
+        cfg = ServeCfg()
+        _lib().gcq_serve_default_cfg(C.byref(cfg))
+        if budget_bytes is not None:
+            cfg.budget_bytes = int(budget_bytes)
+        if max_slots:
+            cfg.max_slots = max_slots
+        if threads:
+            cfg.threads = threads
+        if work_log2:
+            cfg.work_log2 = work_log2
+        if timeout_s:
+            cfg.timeout_ns = int(timeout_s * 1e9)
+        if run_limit_s:
+            cfg.run_limit_ns = int(run_limit_s * 1e9)
+        for name, v in work_knobs.items():   # knobs of the worklist queue
+            setattr(cfg.work_knobs, name, v)
+        h = P()
+        _check(_lib().gcq_serve_create(n, C.cast(offs, P), C.cast(idxs, P), self.V.ctypes.data, E.ctypes.data,
+                                       C.byref(cfg), C.byref(h)), "gcq_serve_create")
+        self._h = h
+
+    def info(self, graph: int = -1) -> dict:
+        slots, threads, lb = U32(), U32(), U64()
+        _check(_lib().gcq_serve_info(self._h, graph, C.byref(slots), C.byref(threads), C.byref(lb)),
+               "gcq_serve_info")
+        return {"slots": slots.value, "threads": threads.value, "level_bytes": lb.value}
+
+    def run(self, reqs: np.ndarray):
+        reqs = np.ascontiguousarray(reqs, dtype=SERVE_REQ_DTYPE)
+        res = np.zeros(len(reqs), dtype=SERVE_RES_DTYPE)
+        st = ServeStats()
+        rc = _lib().gcq_serve_run(self._h, reqs.ctypes.data, len(reqs), res.ctypes.data, C.byref(st))
+        self.last_stats = {f: (list(getattr(st, f)) if f.startswith("work_") else getattr(st, f))
+                           for f, _ in ServeStats._fields_}
+        self.last_results = res
+        _check(rc, "gcq_serve_run")
+        return res, self.last_stats
+
+    def close(self):
+        if self._h:
+            _lib().gcq_serve_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def serve_requests(n: int, ngraphs: int, V, rate_per_s: float = 0.0, seed: int = 1, weights=None):
+    """A seeded request schedule: graph drawn by `weights` (uniform by default), a
+    uniform source vertex, Poisson arrivals at `rate_per_s` (0: all at time 0)."""
+    rng = np.random.default_rng(seed)
+    r = np.zeros(n, dtype=SERVE_REQ_DTYPE)
+    p = None if weights is None else np.asarray(weights, dtype=np.float64) / np.sum(weights)
+    r["graph"] = rng.choice(ngraphs, size=n, p=p)
+    r["src"] = (rng.random(n) * np.asarray(V)[r["graph"]]).astype(np.int64)
+    if rate_per_s > 0:
+        r["arrival_ns"] = np.cumsum(rng.exponential(1e9 / rate_per_s, size=n)).astype(np.uint64)
+    return r
 
 
 def rt_render(kind: str = "gwfq", scene: int = 0, width: int = 1280, height: int = 720, tiles_x: int = 8,

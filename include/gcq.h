@@ -296,6 +296,80 @@ typedef struct gcq_roofline {
 /* Run the microbenchmark (best of `reps`); synchronises the device. */
 int gcq_roofline_measure(gcq_roofline* out, int reps);
 
+/* --------------------------------------------------------- served BFS ----
+ * A persistent server of BFS traversal requests over several resident graphs,
+ * built on G-WFQ queues (Enqueue_Ptr/Dequeue_Ptr, gwf_ring.hpp:1362-1380) and the
+ * persistent worker loop of the ray tracer (rt_final.cpp:574-641).  The reference
+ * runs one traversal per process (bfs_bench.cpp:327-496); it has no server.
+ *
+ * Requests arrive on the device clock (arrival_ns after the start of the run).  A
+ * request is admitted when a level-array slot of its graph is free (slots are
+ * carved out of budget_bytes, an even share per graph) and its graph's vertex count
+ * fits the worklist reservation.  Each traversal computes exact hop distances and
+ * returns, instead of the level array, its checksum
+ *     sum over v < V of splitmix64(v << 32 | level(v))   (mod 2^64)
+ * with level 0xFFFFFFFF for unreached vertices, its reached count and its
+ * eccentricity (max_level). */
+typedef struct gcq_server gcq_server;
+
+typedef struct gcq_serve_cfg {
+    uint64_t budget_bytes;  /* HBM for level arrays; default 150 GiB */
+    uint64_t timeout_ns;    /* bound of every device wait; default 10 s */
+    uint32_t max_slots;     /* level-array slots per graph, at most; default 1024 */
+    uint32_t threads;       /* persistent threads; 0 = every resident thread */
+    uint32_t work_log2;     /* worklist capacity; default 25, raised to 2 x the largest graph */
+    uint32_t _pad;
+    uint64_t run_limit_ns;  /* a run gives up (GCQ_ETIMEDOUT) this long after the last
+                               arrival; default 60 s */
+    gcq_knobs work_knobs;   /* knobs of the worklist queue; default gcq_default_knobs */
+} gcq_serve_cfg;
+
+typedef struct gcq_serve_req {
+    int32_t graph;          /* index into the graphs given to gcq_serve_create */
+    int32_t src;            /* source vertex */
+    uint64_t arrival_ns;    /* release time (<= 60 s); requests are sorted by it */
+} gcq_serve_req;
+
+typedef struct gcq_serve_res {
+    uint64_t admit_ns;      /* slot granted */
+    uint64_t done_ns;       /* last vertex settled */
+    uint64_t finish_ns;     /* checksum folded, slot returned (response time) */
+    uint64_t checksum;
+    uint32_t reached;
+    int32_t max_level;
+} gcq_serve_res;
+
+typedef struct gcq_serve_stats {
+    double kernel_ms;       /* CUDA-event time of the persistent kernel */
+    uint64_t items;         /* vertex items dequeued */
+    uint64_t stale;         /* of those, superseded by a shorter path */
+    uint64_t edges;         /* adjacency entries scanned */
+    uint64_t sweeps;        /* checksum/reset sweeps of level arrays */
+    uint32_t completed;
+    uint32_t error_word;
+    uint32_t released;      /* requests moved into submission queues */
+    uint32_t inflight;      /* slots still holding a traversal at the end (0 after success) */
+    uint64_t reserved;      /* worklist reservation left at the end (0 after success) */
+    uint64_t work_tail[2];  /* ticket counters of the worklist's rings at the end: */
+    uint64_t work_head[2];  /*   [0] the item ring, [1] the free-index ring */
+    int32_t work_threshold[2];
+} gcq_serve_stats;
+
+void gcq_serve_default_cfg(gcq_serve_cfg* cfg);
+/* Upload the CSR graphs (host arrays as made by gcq_graph_grid/gcq_graph_rmat) and
+ * allocate slots and queues.  GCQ_EINVAL for a malformed CSR (offsets not starting
+ * at 0, decreasing or not ending at E; a neighbour outside [0, V)); GCQ_ECAPACITY
+ * if one level array of a graph does not fit its share of the budget. */
+int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* const* indices,
+                     const int32_t* V, const int64_t* E, const gcq_serve_cfg* cfg, gcq_server** out);
+int gcq_serve_destroy(gcq_server* s);
+/* Slots of `graph` (-1: all graphs), persistent threads, bytes of level arrays. */
+int gcq_serve_info(const gcq_server* s, int graph, uint32_t* slots, uint32_t* threads, uint64_t* level_bytes);
+/* Serve nreq requests (<= 2^20, sorted by arrival_ns) in one persistent launch;
+ * res[i] answers reqs[i].  Synchronises the device. */
+int gcq_serve_run(gcq_server* s, const gcq_serve_req* reqs, uint32_t nreq, gcq_serve_res* res,
+                  gcq_serve_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

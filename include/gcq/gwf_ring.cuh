@@ -58,6 +58,9 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
 __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j, uint32_t tid) {
     GCQ_STAT(c, stat::FINALIZE);
     const uint64_t h_local = h_raw << 2;
+    // the entry was read relaxed; this fence makes the owner store that preceded
+    // the producing (release) CAS visible, so the lookup does not miss and scan
+    fence_acq_rel();
     const uint32_t own = ld_rlx(&c.owner[j]);
     if (own != 0 && own <= c.max_threads) {
         const uint64_t lt = ld_acq(&c.rec[own - 1].localTail);
@@ -288,7 +291,13 @@ __device__ inline bool try_enq_slow(ring* q, const cfg& c, uint64_t T_raw, uint3
             if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
             return true;
         }
-        return cycle_cmp(ecyc, tcyc) == 0;
+        // The slot is at our cycle: produced for this request (our index, or
+        // consumed since, index ⊥c) -- or passed by the dequeuer that holds the same
+        // ticket, which marks it ⊥ at our cycle.  gwf_ring.hpp:697-704 takes every
+        // cycle match as "already produced", which loses the element in the second
+        // case; here it fails the ticket, as the fast path does, and the request
+        // takes another.
+        return cycle_cmp(ecyc, tcyc) == 0 && (eidx == index || eidx == BOT_C);
     }
     raise_error(c.err, ERR_SPIN);
     return true;
@@ -333,10 +342,18 @@ __device__ inline bool try_deq_slow(ring* q, const cfg& c, uint64_t H_raw, recor
     return false;
 }
 
-// enqueue_slow / dequeue_slow, gwf_ring.hpp:775-802
-__device__ inline void enqueue_slow(ring* q, const cfg& c, uint64_t v, uint32_t index, record* r, uint32_t tid) {
-    while (slow_faa(q, c, &q->Tail, &r->localTail, &v, nullptr, tid))
+// enqueue_slow / dequeue_slow, gwf_ring.hpp:775-802.  A helper (seq != NO_SEQ)
+// stops once the request it read is over: a request's localTail is published with
+// a release store after the previous request's seq1 increment, so a helper that
+// obtained a ticket from a newer request sees seq1 moved and does not produce the
+// old request's index there.
+constexpr uint32_t NO_SEQ = 0xFFFFFFFFu;
+__device__ inline void enqueue_slow(ring* q, const cfg& c, uint64_t v, uint32_t index, record* r, uint32_t tid,
+                                    uint32_t seq = NO_SEQ) {
+    while (slow_faa(q, c, &q->Tail, &r->localTail, &v, nullptr, tid)) {
+        if (seq != NO_SEQ && ld_acq(&r->seq1) != seq) break;
         if (try_enq_slow(q, c, v >> 2, index, r)) break;
+    }
 }
 __device__ inline void dequeue_slow(ring* q, const cfg& c, uint64_t v, record* r, uint32_t tid) {
     while (slow_faa(q, c, &q->Head, &r->localHead, &v, &q->Threshold, tid))
@@ -351,7 +368,7 @@ __device__ inline void help_enqueue(ring* q, const cfg& c, record* thr, uint32_t
     const uint32_t idx = ld_rlx(&thr->index);
     const uint64_t init_tail = ld_rlx(&thr->initTail);
     fence_acq_rel();
-    if (is_enq && ld_rlx(&thr->seq1) == seq) enqueue_slow(q, c, init_tail, idx, thr, tid);
+    if (is_enq && ld_rlx(&thr->seq1) == seq) enqueue_slow(q, c, init_tail, idx, thr, tid, seq);
 }
 __device__ inline void help_dequeue(ring* q, const cfg& c, record* thr, uint32_t tid) {
     const uint32_t seq = ld_acq(&thr->seq2);
@@ -391,7 +408,7 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
     record* r = &c.rec[tid];
     const uint32_t seq = ld_rlx(&r->seq1);
     const uint64_t tail_local = tail << 2;
-    st_rlx(&r->localTail, tail_local);
+    st_rel(&r->localTail, tail_local);   // after the previous request's seq1 increment
     st_rlx(&r->initTail, tail_local);
     st_rlx(&r->index, index);
     st_rlx(&r->enqueue, 1u);
@@ -437,6 +454,32 @@ __device__ inline uint32_t dequeue(ring* q, uint32_t tid) {
     return BOT;
 }
 
+// A hint for polling consumers, not a queue operation (the reference has none):
+// true when the ring's Tail counter is ahead of its Head counter.  It reads two
+// words and changes nothing, so a consumer that polls an idle queue through it
+// takes no Head ticket, marks no slot and leaves the Threshold alone.  An entry
+// enqueued at ticket T and not yet dequeued implies Head <= T < Tail, so the hint
+// turns true once such an entry exists; it may also be true for an empty queue
+// (a dequeue then simply fails).
+__device__ __forceinline__ bool maybe_nonempty(const ring* q) {
+    const uint32_t b = q->thr_bits;
+    return (ld_rlx(&q->Tail) >> b) > (ld_rlx(&q->Head) >> b);
+}
+
+// Dequeue for polling consumers (the reference has none): at most `tries` fast-path
+// attempts, no help record, no slow path.  BOT when they find the queue empty or
+// run out; the caller polls again.  A consumer that polls an idle queue through
+// the wait-free dequeue publishes a slow-path request after deq_patience failures,
+// and with many pollers those requests race the dequeue front without end.
+__device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
+    if (ld_rlx(&q->Threshold) < 0) return BOT;
+    const cfg c = load_cfg(q);
+    uint32_t out = BOT;
+    for (uint32_t k = 0; k < tries; ++k)
+        if (try_deq(q, c, &out, tid) == 0) return out;
+    return BOT;
+}
+
 // Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.
 __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
     const uint32_t idx = dequeue(&q->fq, tid);
@@ -450,6 +493,14 @@ __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid
     if (idx == BOT) return false;
     *out = ld_rlx(&q->data[idx]);
     enqueue(&q->fq, idx, tid);   // releases the slot only after the read above
+    return true;
+}
+// try_dequeue on the item ring of an MPMC queue.
+__device__ __forceinline__ bool try_dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid, uint32_t tries) {
+    const uint32_t idx = try_dequeue(&q->aq, tid, tries);
+    if (idx == BOT) return false;
+    *out = ld_rlx(&q->data[idx]);
+    enqueue(&q->fq, idx, tid);
     return true;
 }
 

@@ -31,3 +31,22 @@ extern "C" int32_t oracle_bfs(int32_t V, const int32_t* offsets, const int32_t* 
     }
     return maxl;   // eccentricity of src within its component
 }
+
+// Checksum of a level array as the served traversals report it: the sum (mod 2^64)
+// over v of splitmix64(v << 32 | level), level 0xFFFFFFFF where unreached (-1).
+// splitmix64 is Steele, Lea and Flood's SplitMix64 finaliser (OOPSLA 2014).
+static uint64_t splitmix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ULL;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+    return x ^ (x >> 31);
+}
+
+extern "C" uint64_t oracle_levels_checksum(int32_t V, const int32_t* level) {
+    uint64_t s = 0;
+    for (int32_t v = 0; v < V; ++v) {
+        const uint32_t l = level[v] < 0 ? 0xFFFFFFFFu : (uint32_t)level[v];
+        s += splitmix64(((uint64_t)(uint32_t)v << 32) | l);
+    }
+    return s;
+}

@@ -102,6 +102,9 @@ struct Ring {
     int thr_bits = 0;
     u64 null_tid = 0, cinc = 0;
     Knobs k;
+    // true: gwf_ring.hpp:697-704 verbatim (a cycle match counts as produced even
+    // when the slot was passed by a dequeuer); false: the corrected rule
+    bool reference_produced_rule = false;
     std::unique_ptr<std::atomic<u64>[]> Entry;
     std::unique_ptr<Rec[]> Record;
 
@@ -307,7 +310,10 @@ struct Ring {
             } else if (ccmp(ec, tc) != 0) {
                 return false;
             }
-            return true;
+            // at our cycle: produced for this request (our index or consumed, ⊥c),
+            // or passed by the dequeuer holding the same ticket (⊥), which the
+            // reference also counts as produced
+            return reference_produced_rule || ei == index || ei == BOT_C;
         }
     }
     bool try_deq_slow(u64 H, Rec& r) {
@@ -344,9 +350,13 @@ struct Ring {
         }
         return false;
     }
-    void enqueue_slow(u64 v, u32 index, Rec& r, u32 me) {
-        while (slow_faa(&Tail, &r.localTail, &v, nullptr, me))
+    static constexpr u32 NO_SEQ = 0xFFFFFFFFu;
+    // a helper (seq != NO_SEQ) stops once the request it read is over
+    void enqueue_slow(u64 v, u32 index, Rec& r, u32 me, u32 seq = NO_SEQ) {
+        while (slow_faa(&Tail, &r.localTail, &v, nullptr, me)) {
+            if (seq != NO_SEQ && r.seq1.load() != seq) break;
             if (try_enq_slow(v >> 2, index, r)) break;
+        }
     }
     void dequeue_slow(u64 v, Rec& r, u32 me) {
         while (slow_faa(&Head, &r.localHead, &v, &Threshold, me))
@@ -359,7 +369,7 @@ struct Ring {
         u32 is_enq = t.enqueue.load();
         u32 index = t.index.load();
         u64 it = t.initTail.load();
-        if (is_enq && t.seq1.load() == seq) enqueue_slow(it, index, t, me);
+        if (is_enq && t.seq1.load() == seq) enqueue_slow(it, index, t, me, seq);
     }
     void help_dequeue(Rec& t, u32 me) {
         u32 seq = t.seq2.load();
@@ -1190,6 +1200,39 @@ int oracle_fifo_check(int kind, uint32_t order, uint32_t threads, uint32_t ops_p
         out_counts[2] = dup.load(); out_counts[3] = ord; out_counts[4] = missing + oob.load();
     }
     return (consumed.load() >= total && !dup && !missing && !oob && !ord) ? 0 : 1;
+}
+
+
+// Known-answer case for the slow-path "already produced" rule, one thread, no
+// timing: an enqueuer takes Tail ticket T; the dequeuer that takes Head ticket T
+// finds the slot empty and marks it (cycle(T), ⊥); the enqueuer's slow path then
+// tries ticket T.  Returns what try_enq_slow reports for ticket T (1 = "done") and,
+// in *deq_out, what a dequeue returns after the slow path has run to completion
+// (the index, or ⊥ = 0xFFFFFFFE if the element was lost).
+// reference_rule = 1 runs the rule of gwf_ring.hpp:697-704.
+int oracle_gwf_slow_passed_slot(int reference_rule, uint32_t* deq_out) {
+    gwf::Ring q;
+    q.init(8, 4, 2, gwf::Knobs());
+    q.reference_produced_rule = reference_rule != 0;
+    const u64 T = q.cnt_of(q.Tail.fetch_add(q.cinc));   // enqueuer (thread 0) takes T
+    u32 out = 0;
+    const u64 H = q.try_deq(&out, 1);                   // dequeuer (thread 1) takes T too
+    if (H != 0 || out != gwf::BOT) return -1;
+    const u32 index = 5;
+    gwf::Rec& r = q.Record[0];
+    const u32 seq = r.seq1.load();
+    r.localTail.store(T << 2);
+    r.initTail.store(T << 2);
+    r.index.store(index);
+    r.enqueue.store(1);
+    r.seq2.store(seq);
+    r.pending.store(1);
+    const bool done_at_T = q.try_enq_slow(T, index, r);
+    if (!done_at_T) q.enqueue_slow(T << 2, index, r, 0);
+    r.pending.store(0);
+    r.seq1.store(seq + 1);
+    if (deq_out) *deq_out = q.dequeue_wf(2);
+    return done_at_T ? 1 : 0;
 }
 
 }  // extern "C"

@@ -73,7 +73,33 @@ def lib():
 _EXTRA = [
     ("oracle_bfs", [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int32),
     ("oracle_rt_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p], C.c_int64),
+    ("oracle_levels_checksum", [C.c_int32, C.c_void_p], C.c_uint64),
+    ("oracle_gwf_slow_passed_slot", [C.c_int, C.c_void_p], C.c_int),
 ]
+
+
+# ------------------------------------------------------------------ BFS
+def bfs(offsets: np.ndarray, indices: np.ndarray, src: int):
+    """Serial BFS depths (-1 unreached) and the eccentricity of src."""
+    off = np.ascontiguousarray(offsets, dtype=np.int32)
+    idx = np.ascontiguousarray(indices, dtype=np.int32)
+    lv = np.empty(len(off) - 1, dtype=np.int32)
+    ecc = lib().oracle_bfs(len(off) - 1, off.ctypes.data, idx.ctypes.data, int(src), lv.ctypes.data)
+    if ecc < 0:
+        raise ValueError("bad source vertex %d" % src)
+    return lv, ecc
+
+
+def levels_checksum(levels: np.ndarray) -> int:
+    """Checksum of a level array as the served traversals report it."""
+    lv = np.ascontiguousarray(levels, dtype=np.int32)
+    return int(lib().oracle_levels_checksum(len(lv), lv.ctypes.data))
+
+
+def bfs_summary(offsets: np.ndarray, indices: np.ndarray, src: int):
+    """(checksum, reached, eccentricity) of one traversal, as a served request answers."""
+    lv, ecc = bfs(offsets, indices, src)
+    return levels_checksum(lv), int(np.count_nonzero(lv >= 0)), int(ecc)
 
 
 # ------------------------------------------------------------------ histories

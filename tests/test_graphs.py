@@ -1,0 +1,71 @@
+"""Host-side graph generators and the served-BFS checksum (no GPU calls)."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def gcq_host():
+    import gcq_gb300
+    from gcq_gb300 import build
+    build.build()
+    return gcq_gb300
+
+
+def _check_csr(off, idx):
+    V = len(off) - 1
+    assert off[0] == 0 and off[-1] == len(idx)
+    assert (np.diff(off) >= 0).all()
+    assert ((idx >= 0) & (idx < V)).all()
+    src = np.repeat(np.arange(V), np.diff(off))
+    assert (src != idx).all(), "self loop"
+    for v in range(0, V, max(1, V // 200)):
+        row = idx[off[v]:off[v + 1]]
+        assert (np.diff(row) > 0).all(), "unsorted or duplicate neighbours"
+    fwd = set(zip(src.tolist(), idx.tolist()))
+    assert all((b, a) in fwd for a, b in list(fwd)[:20000]), "not undirected"
+
+
+def test_rmat_shape_and_determinism(gcq_host):
+    off, idx = gcq_host.graph_rmat(10, 16, seed=7)
+    assert len(off) == 1025
+    _check_csr(off, idx)
+    off2, idx2 = gcq_host.graph_rmat(10, 16, seed=7)
+    assert np.array_equal(off, off2) and np.array_equal(idx, idx2)
+    off3, idx3 = gcq_host.graph_rmat(10, 16, seed=8)
+    assert not (np.array_equal(off, off3) and np.array_equal(idx, idx3))
+    deg = np.diff(off)
+    assert deg.max() > 8 * max(1.0, deg.mean())   # skewed degrees
+
+
+def test_grid_shape(gcq_host):
+    off, idx = gcq_host.graph_grid(40, 50, 1.0, 0.0, 0)
+    _check_csr(off, idx)
+    assert len(idx) == 2 * (40 * 49 + 39 * 50)    # every 4-neighbour edge, both directions
+    off, idx = gcq_host.graph_grid(40, 50, 0.6, 0.01, 2)
+    _check_csr(off, idx)
+
+
+def _splitmix64(x):
+    x = (x + np.uint64(0x9E3779B97F4A7C15))
+    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return x ^ (x >> np.uint64(31))
+
+
+def test_levels_checksum_restatement(oracle_lib):
+    rng = np.random.default_rng(1)
+    lv = rng.integers(-1, 50, size=5000).astype(np.int32)
+    v = np.arange(len(lv), dtype=np.uint64)
+    l = np.where(lv < 0, np.uint64(0xFFFFFFFF), lv.astype(np.uint64))
+    with np.errstate(over="ignore"):
+        want = int(np.sum(_splitmix64((v << np.uint64(32)) | l), dtype=np.uint64))
+    assert oracle_lib.levels_checksum(lv) == want
+
+
+def test_bfs_summary(oracle_lib):
+    # path 0-1-2, isolated 3
+    off = np.array([0, 1, 3, 4, 4], np.int32)
+    idx = np.array([1, 0, 2, 1], np.int32)
+    cs, reached, ecc = oracle_lib.bfs_summary(off, idx, 0)
+    assert (reached, ecc) == (3, 2)
+    assert cs == oracle_lib.levels_checksum(np.array([0, 1, 2, -1], np.int32))

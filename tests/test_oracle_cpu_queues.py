@@ -39,3 +39,16 @@ def test_cpu_throughput_counts(oracle_lib):
     # balanced: every thread enqueues then dequeues; at most `threads` values stay queued
     assert r["enq_success"] > 0
     assert r["enq_success"] - r["deq_success"] <= 4 + 64 * 4
+
+
+def test_gwfq_slow_path_passed_slot(oracle_lib):
+    """A slow-path enqueue whose ticket's slot was already passed (marked ⊥ at the
+    same cycle) by a dequeuer: the reference's rule (gwf_ring.hpp:697-704) reports
+    the enqueue done and the element is lost; the corrected rule takes a new ticket
+    and the element is dequeued."""
+    import ctypes
+    out = ctypes.c_uint32(0)
+    assert oracle_lib.lib().oracle_gwf_slow_passed_slot(1, ctypes.byref(out)) == 1
+    assert out.value == 0xFFFFFFFE        # lost: the queue is empty
+    assert oracle_lib.lib().oracle_gwf_slow_passed_slot(0, ctypes.byref(out)) == 0
+    assert out.value == 5                 # delivered
