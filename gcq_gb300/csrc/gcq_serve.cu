@@ -532,8 +532,10 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
     // queues: the worklist holds at least twice the largest graph and every thread;
     // control queues are used by one lane per warp (identity = warp index)
     gcq_knobs k = cfg->work_knobs;   // the control queues follow the worklist's knobs
+    // reservations may reach half the worklist, and that half holds two traversals
+    // of the largest graph, so no graph waits for the worklist to drain completely
     uint32_t work_log2 = cfg->work_log2 ? cfg->work_log2 : 25;
-    work_log2 = std::max({work_log2, log2_ceil((uint64_t)maxV) + 1, log2_ceil(threads)});
+    work_log2 = std::max({work_log2, log2_ceil((uint64_t)maxV) + 2, log2_ceil(threads)});
     if (work_log2 > 30) return fail(GCQ_ECAPACITY);
     s->work_cap = 1ull << work_log2;
     gcq_queue* q = nullptr;

@@ -317,7 +317,7 @@ typedef struct gcq_serve_cfg {
     uint64_t timeout_ns;    /* bound of every device wait; default 10 s */
     uint32_t max_slots;     /* level-array slots per graph, at most; default 1024 */
     uint32_t threads;       /* persistent threads; 0 = every resident thread */
-    uint32_t work_log2;     /* worklist capacity; default 25, raised to 2 x the largest graph */
+    uint32_t work_log2;     /* worklist capacity; default 25, raised to 4 x the largest graph */
     uint32_t _pad;
     uint64_t run_limit_ns;  /* a run gives up (GCQ_ETIMEDOUT) this long after the last
                                arrival; default 60 s */
