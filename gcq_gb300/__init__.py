@@ -109,6 +109,7 @@ SIGNATURES = {
     "gcq_error_word": ([P, C.POINTER(U32), I32], I32),
     "gcq_device_bytes": ([P], U64),
     "gcq_info": ([P, C.POINTER(I32), C.POINTER(U32), C.POINTER(U32)], I32),
+    "gcq_device_info": ([C.c_char_p, I32, C.POINTER(I32)], I32),
     "gcq_strerror": ([I32], C.c_char_p),
     "gcq_last_cuda_error": ([], C.c_char_p),
     "gcq_run_history": ([P, U32, U32, U32, I32, I32, I32, P, SZ, C.POINTER(SZ), P], I32),
@@ -124,6 +125,8 @@ SIGNATURES = {
     "gcq_free": ([P], None),
     "gcq_graph_rmat": ([U32, U32, C.c_double, C.c_double, C.c_double, U64, C.POINTER(P), C.POINTER(P),
                         C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
+    "gcq_graph_load_mtx": ([C.c_char_p, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
+    "gcq_graph_load_snap": ([C.c_char_p, C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int32), C.POINTER(C.c_int64)], I32),
     "gcq_bfs_create": ([I32, P, P, C.c_int32, C.c_int64, U32, U32, C.POINTER(Knobs), C.POINTER(P)], I32),
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
@@ -312,6 +315,20 @@ def graph_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.
     V, E = C.c_int32(), C.c_int64()
     _check(_lib().gcq_graph_rmat(scale, edge_factor, a, b, c, seed, C.byref(po), C.byref(pi),
                                  C.byref(V), C.byref(E)), "gcq_graph_rmat")
+    off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int32)), shape=(V.value + 1,)).copy()
+    idx = np.ctypeslib.as_array(C.cast(pi, C.POINTER(C.c_int32)), shape=(max(E.value, 1),))[: E.value].copy()
+    _lib().gcq_free(po)
+    _lib().gcq_free(pi)
+    return off, idx
+
+
+def graph_load(path: str):
+    """CSR int32 arrays of a MatrixMarket (.mtx) file or a SNAP edge list (any other
+    name), as the BFS harness reads them (gcq_graph_load_mtx / gcq_graph_load_snap)."""
+    po, pi = P(), P()
+    V, E = C.c_int32(), C.c_int64()
+    fn = _lib().gcq_graph_load_mtx if path.endswith(".mtx") else _lib().gcq_graph_load_snap
+    _check(fn(path.encode(), C.byref(po), C.byref(pi), C.byref(V), C.byref(E)), "graph_load(%s)" % path)
     off = np.ctypeslib.as_array(C.cast(po, C.POINTER(C.c_int32)), shape=(V.value + 1,)).copy()
     idx = np.ctypeslib.as_array(C.cast(pi, C.POINTER(C.c_int32)), shape=(max(E.value, 1),))[: E.value].copy()
     _lib().gcq_free(po)

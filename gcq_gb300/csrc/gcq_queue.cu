@@ -339,6 +339,19 @@ int gcq_reset(gcq_queue* q, void* stream) {
     return launch_init(q, gcqi::as_stream(stream), false);
 }
 
+int gcq_device_info(char* name, int name_cap, int* sms) {
+    int dev = 0;
+    GCQ_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    GCQ_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (name && name_cap > 0) {
+        strncpy(name, prop.name, (size_t)name_cap - 1);
+        name[name_cap - 1] = '\0';
+    }
+    if (sms) *sms = prop.multiProcessorCount;
+    return GCQ_OK;
+}
+
 int gcq_device_ptr(gcq_queue* q, void** dev) {
     if (!q || !dev) return GCQ_EINVAL;
     *dev = q->obj;

@@ -99,6 +99,9 @@ uint64_t gcq_device_bytes(const gcq_queue* q);
 int gcq_stats(gcq_queue* q, uint64_t* out, int clear);
 /* Kind, capacity_log2 and max_threads the queue was created with. */
 int gcq_info(const gcq_queue* q, int* kind, uint32_t* capacity_log2, uint32_t* max_threads);
+/* Name and SM count of the current CUDA device, for harness output lines (the
+ * reference reads hipGetDeviceProperties, throughout_bench.cpp:1058-1062). */
+int gcq_device_info(char* name, int name_cap, int* sms);
 const char* gcq_strerror(int status);
 /* Text of the last failing CUDA call in this process ("" if none). */
 const char* gcq_last_cuda_error(void);
@@ -240,6 +243,16 @@ void gcq_free(void* p);
  * reference, which reads graph files (bfs_bench.cpp:202-243). */
 int gcq_graph_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
                    int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
+
+/* Graph files as the BFS harness reads them (load_mtx / load_snap / csr_from_edges,
+ * bfs_bench.cpp:186-243): a MatrixMarket coordinate file (1-based, V = max(rows,
+ * cols), entries outside the size dropped) or a SNAP edge list ('#'/'%' comments,
+ * ids shifted down when the smallest is 1, V = largest id + 1).  Self loops are
+ * dropped, every edge is stored in both directions, duplicates are removed and each
+ * adjacency list is sorted.  Arrays as for gcq_graph_grid.  GCQ_EINVAL for a
+ * missing or malformed file. */
+int gcq_graph_load_mtx(const char* path, int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
+int gcq_graph_load_snap(const char* path, int32_t** offsets, int32_t** indices, int32_t* V, int64_t* E);
 
 /* Upload the CSR and create the two frontier queues of `kind` for `threads`
  * worker threads (a multiple of 32) with capacity 2^capacity_log2 (0 = the

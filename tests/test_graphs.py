@@ -69,3 +69,52 @@ def test_bfs_summary(oracle_lib):
     cs, reached, ecc = oracle_lib.bfs_summary(off, idx, 0)
     assert (reached, ecc) == (3, 2)
     assert cs == oracle_lib.levels_checksum(np.array([0, 1, 2, -1], np.int32))
+
+
+def _csr_from_edges(V, pairs):
+    """csr_from_edges after sort + unique (bfs_bench.cpp:186-200, 222-223), in numpy."""
+    e = sorted(set(pairs))
+    off = np.zeros(V + 1, np.int64)
+    for u, _ in e:
+        off[u + 1] += 1
+    return np.cumsum(off).astype(np.int32), np.array([v for _, v in e], np.int32)
+
+
+def test_load_mtx(gcq_host, tmp_path):
+    p = tmp_path / "g.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate pattern symmetric\n% comment\n"
+                 "6 5 7\n1 2\n2 3\n3 3\n% inline comment\n4 2\n2 1\n7 1\n5 6\n")
+    off, idx = gcq_host.graph_load(str(p))
+    # 3-3 self loop dropped, 7-1 out of range (rows = 6), 5-6: column 6 > cols = 5 dropped,
+    # 2-1 duplicates 1-2; V = max(6, 5)
+    pairs = []
+    for u, v in [(0, 1), (1, 2), (3, 1), (1, 0)]:
+        pairs += [(u, v), (v, u)]
+    want = _csr_from_edges(6, pairs)
+    assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+
+
+def test_load_snap(gcq_host, tmp_path):
+    p = tmp_path / "g.txt"
+    p.write_text("# Directed graph\n# FromNodeId ToNodeId\n1 2\n2 3\n3 1\n4 4\n5 3\n2 3\n")
+    off, idx = gcq_host.graph_load(str(p))
+    # smallest id is 1: shifted down; V = 5; 4-4 dropped
+    pairs = []
+    for u, v in [(0, 1), (1, 2), (2, 0), (4, 2), (1, 2)]:
+        pairs += [(u, v), (v, u)]
+    want = _csr_from_edges(5, pairs)
+    assert np.array_equal(off, want[0]) and np.array_equal(idx, want[1])
+    p0 = tmp_path / "g0.txt"
+    p0.write_text("0 1\n1 2\n")
+    off, idx = gcq_host.graph_load(str(p0))
+    assert len(off) == 4 and list(idx) == [1, 0, 2, 1]
+
+
+def test_load_rejects(gcq_host, tmp_path):
+    import gcq_gb300
+    bad = tmp_path / "bad.mtx"
+    bad.write_text("not a matrix market file\n1 2\n")
+    with pytest.raises(gcq_gb300.GcqError):
+        gcq_host.graph_load(str(bad))
+    with pytest.raises(gcq_gb300.GcqError):
+        gcq_host.graph_load(str(tmp_path / "missing.mtx"))
