@@ -10,7 +10,7 @@
 // dequeuer waits briefly for the enqueuer holding its ticket before marking the
 // slot (deq_wait);
 // the permutation spreads over 128-byte lines (16 entries) by default; Tail, Head
-// and Threshold own separate lines; loads are acquire/relaxed loads instead of
+// and Threshold sit GCQ_HOT_STRIDE apart; loads are acquire/relaxed loads instead of
 // atomicAdd(p, 0) (:144-148); retry loops are bounded (GCQ_SPIN_LIMIT) and report
 // through the header's error word instead of spinning forever.
 #pragma once
@@ -53,11 +53,11 @@ __host__ __device__ __forceinline__ int cycle_cmp(uint32_t a, uint32_t b) {
 
 struct alignas(128) ring {
     u64a Tail;
-    char _pad0[120];
+    char _pad0[GCQ_HOT_STRIDE - 8];
     u64a Head;
-    char _pad1[120];
+    char _pad1[GCQ_HOT_STRIDE - 8];
     int Threshold;
-    char _pad2[124];
+    char _pad2[GCQ_HOT_STRIDE - 4];
     u64a* Entry;          // 2N slots
     u32a* err;
     uint32_t order;       // log2 N

@@ -124,15 +124,15 @@ struct helper_state {
     uint32_t nextTid;
 };
 
-// Ring header.  The three hot words sit on separate lines; the parameters after
-// them are written once by init and only read afterwards.
+// Ring header.  The three hot words sit GCQ_HOT_STRIDE apart; the parameters
+// after them are written once by init and only read afterwards.
 struct alignas(128) ring {
     u64a Tail;
-    char _pad0[120];
+    char _pad0[GCQ_HOT_STRIDE - 8];
     u64a Head;
-    char _pad1[120];
+    char _pad1[GCQ_HOT_STRIDE - 8];
     int Threshold;
-    char _pad2[124];
+    char _pad2[GCQ_HOT_STRIDE - 4];
     u64a* Entry;            // 2N slots
     record* Record;         // max_threads shared records
     helper_state* Help;     // max_threads private countdowns

@@ -35,11 +35,11 @@ namespace sfq {
 
 struct alignas(128) queue {
     u32a head;
-    char _pad0[124];
+    char _pad0[GCQ_HOT_STRIDE - 4];
     u32a tail;
-    char _pad1[124];
+    char _pad1[GCQ_HOT_STRIDE - 4];
     u32a closed;
-    char _pad2[124];
+    char _pad2[GCQ_HOT_STRIDE - 4];
     u64a* slot;            // L words {id << 32 | item}
     u32a* err;
     uint32_t log2_len;     // L = 1 << log2_len

@@ -75,9 +75,9 @@ struct alignas(64) handle {
 
 struct alignas(128) queue {
     u64a T;
-    char _pad0[120];
+    char _pad0[GCQ_HOT_STRIDE - 8];
     u64a H;
-    char _pad1[120];
+    char _pad1[GCQ_HOT_STRIDE - 8];
     cell* cells;
     handle* handles;
     u32a* err;
