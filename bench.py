@@ -329,7 +329,7 @@ def run_served(args):
     E = [len(i) for _, i in graphs]
     reqs = g.serve_requests(args.serve_requests, len(graphs), V, rate_per_s=args.serve_rate, seed=7)
     peaks = g.roofline(reps=2)
-    srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0)
+    srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0, threads=args.serve_threads)
     info = srv.info()
     for _ in range(args.warmup):
         srv.run(reqs)
@@ -432,6 +432,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=0.0, help="Poisson arrivals per second (0: closed batch)")
     ap.add_argument("--serve-scales", default="16,17,18,19,20,21,22")
     ap.add_argument("--serve-sample", type=int, default=3)
+    ap.add_argument("--serve-threads", type=int, default=65536, help="persistent server threads (0: all resident)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

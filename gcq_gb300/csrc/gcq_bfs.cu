@@ -198,6 +198,217 @@ __global__ void k_bfs_source(void* q, int* level, int src, bfs_misc* m) {
     }
 }
 
+// ------------------------------------------------------------- asynchronous form
+// One persistent launch, one queue, no level barrier: a label-correcting BFS.  An
+// item is (level << 32 | vertex); a vertex of more than ASYNC_HUB_DEG neighbours is
+// expanded as chunk items (1 << 63 | chunk << 32 | vertex) of CHUNK_EDGES edges each,
+// so many warps share a hub; a chunk relaxes with the vertex's current level.  Relaxing an edge lowers the neighbour's level
+// with atomicMin on the unsigned level (unvisited -1 is above every level) and
+// queues it when it dropped; an item whose vertex already has a smaller level is
+// stale.  The final levels are exact hop distances in any processing order.  A
+// pending count (items queued, not yet settled; one update per item, by
+// children - 1) ends the traversal at zero.  The reference has no such form: its
+// traversal synchronises the grid once per level (bfs_bench.cpp:583-623), which
+// bounds it below by levels x barrier latency on high-diameter graphs.
+constexpr int ASYNC_HUB_DEG = 2048;
+constexpr int CHUNK_EDGES = 1024;
+constexpr uint64_t CHUNK_FLAG = 1ull << 63;
+
+struct bfs_async_ctl {
+    unsigned long long pending;
+    unsigned int done;
+    unsigned int err;
+    unsigned long long edges;
+    unsigned long long items, stale;
+    unsigned long long deadline_ns;
+    unsigned long long timeout_ns;
+};
+
+template <int K> struct async_q;
+template <> struct async_q<GCQ_GWFQ> {
+    using Q = gcq::gwf::mpmc;
+    __device__ static bool peek(Q* q) { return gcq::gwf::maybe_nonempty(&q->aq); }
+    __device__ static bool deq(Q* q, uint64_t* v, uint32_t tid) { return gcq::gwf::try_dequeue_ptr(q, v, tid, 2); }
+    __device__ static bool enq(Q* q, uint64_t v, uint32_t tid) { return gcq::gwf::enqueue_ptr_lockfree(q, v, tid, 64); }
+    __device__ static uint64_t mark(Q* q) { return gcq::ld_rlx(&q->aq.Tail); }
+};
+template <> struct async_q<GCQ_GLFQ> {
+    using Q = gcq::glf::mpmc;
+    __device__ static bool peek(Q* q) { return gcq::ld_rlx(&q->aq.Tail) > gcq::ld_rlx(&q->aq.Head); }
+    __device__ static bool deq(Q* q, uint64_t* v, uint32_t) { return gcq::glf::dequeue_ptr(q, v); }
+    __device__ static bool enq(Q* q, uint64_t v, uint32_t) { return gcq::glf::enqueue_ptr(q, v); }
+    __device__ static uint64_t mark(Q* q) { return gcq::ld_rlx(&q->aq.Tail); }
+};
+
+template <int K>
+__device__ __forceinline__ void async_push(typename async_q<K>::Q* q, uint64_t it, uint32_t tid, bfs_async_ctl* c) {
+    if (async_q<K>::enq(q, it, tid)) return;
+    const uint64_t t0 = gcq::globaltimer_ns();
+    uint32_t ns = 32;
+    do {
+        if (gcq::globaltimer_ns() - t0 > c->timeout_ns) { gcq::raise_error(&c->err, gcq::ERR_CAPACITY); return; }
+        __nanosleep(ns);
+        ns = ns < 2048 ? ns * 2 : ns;
+    } while (!async_q<K>::enq(q, it, tid));
+}
+
+__device__ __forceinline__ void async_settle(bfs_async_ctl* c, uint32_t children) {
+    if (children == 1) return;   // the child inherits the item's count
+    const uint64_t prev = gcq::fetch_add((gcq::u64a*)&c->pending, (uint64_t)children - 1);
+    if (children == 0 && prev == 1) gcq::st_rel((gcq::u32a*)&c->done, 1u);
+}
+
+template <int K>
+__global__ void __launch_bounds__(256) k_bfs_async(void* qv, const int* __restrict__ off, const int* __restrict__ idx,
+                                                   unsigned int* __restrict__ level, bfs_async_ctl* c) {
+    using Q = typename async_q<K>::Q;
+    Q* q = (Q*)qv;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = (int)(threadIdx.x & 31);
+    const unsigned FULL = 0xffffffffu;
+    unsigned long long n_edges = 0, n_items = 0, n_stale = 0;
+    uint64_t idle_since = 0, idle_mark = 0;
+    uint32_t ns = 0;
+    for (;;) {
+        uint32_t stop = 0;
+        if (lane == 0) {
+            stop = (gcq::ld_acq((const gcq::u32a*)&c->done) || gcq::ld_rlx((const gcq::u32a*)&c->err)) ? 1u : 0u;
+            if (!stop && gcq::globaltimer_ns() > c->deadline_ns) {
+                gcq::raise_error(&c->err, gcq::ERR_TIMEOUT);
+                stop = 1;
+            }
+        }
+        if (__shfl_sync(FULL, stop, 0)) break;
+        uint64_t it = 0;
+        const bool got = async_q<K>::peek(q) && async_q<K>::deq(q, &it, tid);
+        int big = 0;           // 1: a vertex of 33..ASYNC_HUB_DEG neighbours, 2: a chunk of a hub
+        uint32_t v = 0, lvl = 0;
+        int rb = 0, re = 0;    // edge range of the warp-wide work
+        if (got) {
+            ++n_items;
+            v = (uint32_t)it;
+            if (it & CHUNK_FLAG) {
+                const uint32_t k = (uint32_t)(it >> 32) & 0x7FFFFFFFu;
+                lvl = gcq::ld_rlx((const gcq::u32a*)&level[v]);
+                const int beg = off[v], end = off[v + 1];
+                rb = beg + (int)k * CHUNK_EDGES;
+                re = min(end, rb + CHUNK_EDGES);
+                big = 2;
+            } else if (lvl = (uint32_t)(it >> 32), gcq::ld_rlx((const gcq::u32a*)&level[v]) < lvl) {
+                ++n_stale;
+                async_settle(c, 0);
+            } else {
+                const int beg = off[v], end = off[v + 1];
+                if (end - beg > ASYNC_HUB_DEG) {
+                    // split into chunk items; they inherit this item's count
+                    const uint32_t chunks = (uint32_t)((end - beg + CHUNK_EDGES - 1) / CHUNK_EDGES);
+                    gcq::fetch_add((gcq::u64a*)&c->pending, (uint64_t)chunks - 1);
+                    for (uint32_t k = 0; k < chunks; ++k) async_push<K>(q, CHUNK_FLAG | ((uint64_t)k << 32) | v, tid, c);
+                } else if (end - beg > 32) {
+                    rb = beg;
+                    re = end;
+                    big = 1;
+                } else {
+                    n_edges += (unsigned long long)(end - beg);
+                    const uint32_t lv = lvl + 1;
+                    uint32_t won = 0;
+                    for (int e = beg; e < end; ++e)
+                        if (atomicMin(&level[idx[e]], lv) > lv) won |= 1u << (e - beg);
+                    const uint32_t kids = (uint32_t)__popc(won);
+                    if (kids > 1) gcq::fetch_add((gcq::u64a*)&c->pending, (uint64_t)kids - 1);
+                    for (uint32_t mm = won; mm; mm &= mm - 1)
+                        async_push<K>(q, ((uint64_t)lv << 32) | (uint32_t)idx[beg + __ffs(mm) - 1], tid, c);
+                    if (kids == 0) async_settle(c, 0);
+                }
+            }
+        }
+        // vertices of degree > 32 and hub chunks: the whole warp, one at a time
+        for (unsigned want = __ballot_sync(FULL, big != 0); want; want = __ballot_sync(FULL, big != 0)) {
+            const int owner = __ffs(want) - 1;
+            const uint32_t lv = __shfl_sync(FULL, lvl, owner) + 1;
+            const int beg = __shfl_sync(FULL, rb, owner), end = __shfl_sync(FULL, re, owner);
+            if (lane == owner) n_edges += (unsigned long long)(end - beg);
+            for (int base = beg; base < end; base += 32) {
+                const int e = base + lane;
+                uint32_t w = 0;
+                bool won = false;
+                if (e < end) {
+                    w = (uint32_t)idx[e];
+                    won = atomicMin(&level[w], lv) > lv;
+                }
+                const unsigned wm = __ballot_sync(FULL, won);
+                // count the children before any of them can be dequeued
+                if (lane == owner && wm) gcq::fetch_add((gcq::u64a*)&c->pending, (uint64_t)__popc(wm));
+                __syncwarp();
+                if (won) async_push<K>(q, ((uint64_t)lv << 32) | w, tid, c);
+            }
+            if (lane == owner) {
+                async_settle(c, 0);
+                big = 0;
+            }
+        }
+        if (got) {
+            ns = 0;
+            idle_since = 0;
+        } else {
+            // stall detection: no enqueue anywhere for a whole timeout
+            const uint64_t t = gcq::globaltimer_ns();
+            const uint64_t mk = async_q<K>::mark(q);
+            if (idle_since == 0 || mk != idle_mark) {
+                idle_since = t;
+                idle_mark = mk;
+            } else if (t - idle_since > c->timeout_ns) {
+                gcq::raise_error(&c->err, gcq::ERR_TIMEOUT);
+            }
+            if (ns) __nanosleep(ns);
+            ns = ns ? (ns < 1024 ? ns * 2 : ns) : 32;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_edges += __shfl_xor_sync(FULL, n_edges, o);
+        n_items += __shfl_xor_sync(FULL, n_items, o);
+        n_stale += __shfl_xor_sync(FULL, n_stale, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&c->edges, n_edges);
+        atomicAdd(&c->items, n_items);
+        atomicAdd(&c->stale, n_stale);
+    }
+}
+
+__global__ void k_bfs_set_deadline(bfs_async_ctl* c, uint64_t after_ns) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->deadline_ns = gcq::globaltimer_ns() + after_ns;
+}
+
+template <int K>
+__global__ void k_bfs_async_source(void* qv, unsigned int* level, int src, bfs_async_ctl* c) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        level[src] = 0;
+        c->pending = 1;
+        if (!async_q<K>::enq((typename async_q<K>::Q*)qv, (uint32_t)src, 0)) gcq::raise_error(&c->err, gcq::ERR_CAPACITY);
+    }
+}
+
+// reached vertices and the largest level, for the asynchronous form
+__global__ void k_bfs_summary(const int* __restrict__ level, int V, bfs_misc* m) {
+    unsigned int reached = 0, maxl = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const int l = level[v];
+        if (l >= 0) {
+            ++reached;
+            maxl = max(maxl, (unsigned)l);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        reached += __shfl_xor_sync(0xffffffffu, reached, o);
+        maxl = max(maxl, __shfl_xor_sync(0xffffffffu, maxl, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&m->reached, reached);
+        atomicMax(&m->levels, maxl + 1);
+    }
+}
+
 // Grid barrier for the persistent form: every block of a cooperative launch arrives
 // once per phase; the wait is bounded and reports through m->err.
 __device__ __forceinline__ bool grid_barrier(bfs_misc* m, uint64_t timeout_ns) {
@@ -332,8 +543,12 @@ int gcq_bfs_create(int kind, const int32_t* offsets, const int32_t* indices, int
     if (!offsets || !indices || !out || V <= 0 || E < 0 || threads == 0 || (threads & 31)) return GCQ_EINVAL;
     *out = nullptr;
     if (capacity_log2 == 0) {
+        // the whole graph (a frontier never holds more), and at least the thread
+        // count, which G-WFQ requires (max_threads <= capacity, gwf_queue.hpp:320)
         capacity_log2 = 15;
         while ((1ull << capacity_log2) < (uint64_t)V && capacity_log2 < 26) ++capacity_log2;
+        if (kind == GCQ_GWFQ)
+            while ((1ull << capacity_log2) < (uint64_t)threads && capacity_log2 < 26) ++capacity_log2;
         if (kind == GCQ_SFQ)   // SFQ's MAX_ID envelope: L <= 2^32 / (threads + 1)
             while (capacity_log2 > 10 && (1ull << capacity_log2) > (1ull << 32) / ((uint64_t)threads + 1))
                 --capacity_log2;
@@ -408,11 +623,12 @@ int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int
     int rc = gcq_reset(c->qa, s);
     if (rc == GCQ_OK) rc = gcq_reset(c->qb, s);
     if (rc != GCQ_OK) return rc;
-    rc = dispatch(c->kind, [&](auto kc) {
-        constexpr int K = decltype(kc)::value;
-        k_bfs_source<K><<<1, 32, 0, s>>>(c->qa->obj, c->d_level, src, m);
-        return GCQ_OK;
-    });
+    if (persistent != 2)   // the asynchronous form queues its own (level, vertex) source item
+        rc = dispatch(c->kind, [&](auto kc) {
+            constexpr int K = decltype(kc)::value;
+            k_bfs_source<K><<<1, 32, 0, s>>>(c->qa->obj, c->d_level, src, m);
+            return GCQ_OK;
+        });
     GCQ_CUDA(cudaGetLastError());
     GCQ_CUDA(cudaStreamSynchronize(s));
     out->init_ms = std::chrono::duration<double, std::milli>(clk::now() - t_total).count();
@@ -456,6 +672,38 @@ int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int
             std::swap(qin, qout);
         }
         out->edges_scanned = hm->edges;
+    } else if (persistent == 2) {
+        // asynchronous label-correcting form: G-WFQ and G-LFQ (64-bit items)
+        if (c->kind != GCQ_GWFQ && c->kind != GCQ_GLFQ) return GCQ_EUNSUPPORTED;
+        bfs_async_ctl* ac = (bfs_async_ctl*)((char*)c->d_misc + 128);
+        bfs_async_ctl hac;
+        memset(&hac, 0, sizeof hac);
+        hac.timeout_ns = 5000000000ull;
+        GCQ_CUDA(cudaMemcpyAsync(ac, &hac, sizeof hac, cudaMemcpyHostToDevice, s));
+        cudaEventRecord(e0, s);
+        rc = dispatch(c->kind, [&](auto kc) {
+            constexpr int K = decltype(kc)::value;
+            if constexpr (K == GCQ_GWFQ || K == GCQ_GLFQ) {
+                k_bfs_async_source<K><<<1, 32, 0, s>>>(c->qa->obj, (unsigned int*)c->d_level, src, ac);
+                k_bfs_set_deadline<<<1, 32, 0, s>>>(ac, 60000000000ull);
+                k_bfs_async<K><<<grid, block, 0, s>>>(c->qa->obj, c->d_off, c->d_idx, (unsigned int*)c->d_level, ac);
+            }
+            return GCQ_OK;
+        });
+        cudaEventRecord(e1, s);
+        k_bfs_summary<<<gcqi::grid_for((uint64_t)c->V, 256), 256, 0, s>>>(c->d_level, c->V, m);
+        GCQ_CUDA(cudaMemcpyAsync(hm, m, 64, cudaMemcpyDeviceToHost, s));
+        GCQ_CUDA(cudaMemcpyAsync(&hac, ac, sizeof hac, cudaMemcpyDeviceToHost, s));
+        GCQ_CUDA(cudaStreamSynchronize(s));
+        GCQ_CUDA(cudaGetLastError());
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        kernel_ms = ms;
+        levels = hm->levels;
+        reached = hm->reached;
+        max_frontier = 0;
+        out->edges_scanned = hac.edges;
+        hm->err |= hac.err;
     } else {
         if (c->kind == GCQ_WFQ) return GCQ_EUNSUPPORTED;   // needs the per-level pool reset
         // cooperative launch: all blocks must be resident for the grid barrier
@@ -503,7 +751,7 @@ int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int
     if (hm->drops) return GCQ_ECAPACITY;
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
-    if (err & GCQ_ERR_POOL) return GCQ_ECAPACITY;
+    if (err & (GCQ_ERR_POOL | GCQ_ERR_CAPACITY)) return GCQ_ECAPACITY;
     return GCQ_OK;
 }
 

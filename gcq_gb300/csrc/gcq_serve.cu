@@ -42,6 +42,12 @@ constexpr uint32_t MAX_LEVEL = CLEANUP - 1;
 constexpr uint32_t MAX_SLOTS = 1u << SLOT_BITS;
 constexpr uint32_t SWEEP = 1u << 13;                  // vertices per sweep item
 constexpr int WARP_DEG = 32;
+// A vertex of more than HUB_DEG neighbours is expanded as chunk items of
+// CHUNK_EDGES edges (vertex field | CHUNK_BIT, chunk index in the level field), so
+// many warps share a hub; a chunk relaxes with the vertex's current level.
+constexpr int HUB_DEG = 2048;
+constexpr int CHUNK_EDGES = 1024;
+constexpr uint32_t CHUNK_BIT = 1u << 31;
 constexpr int MAX_GRAPHS = 64;
 constexpr uint32_t MAX_REQ = 1u << 20;
 constexpr uint64_t MAX_ARRIVAL_NS = 60000000000ull;   // schedules span at most a minute
@@ -243,14 +249,24 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
         // them two loads, not a Head ticket and a marked slot each
         const bool got = gcq::gwf::maybe_nonempty(&x.workq->aq) &&
                          gcq::gwf::try_dequeue_ptr(x.workq, &it, tid, POLL_TRIES);
-        int big = 0;   // 1: edges of a high-degree vertex, 2: a cleanup sweep
+        int big = 0;   // 1: an edge range of one vertex (lvl = the level it gives), 2: a cleanup sweep
         uint32_t slot = 0, lvl = 0, v = 0;
+        int rb = 0, re = 0;
         if (got) {
             slot = item_slot(it);
             lvl = item_lvl(it);
             v = item_v(it);
             if (lvl == CLEANUP) {
                 big = 2;
+            } else if (v & CHUNK_BIT) {
+                ++n_items;
+                srv_slot* s = &x.slots[slot];
+                const srv_graph& g = x.graphs[s->graph];
+                const uint32_t u = v & ~CHUNK_BIT;
+                rb = g.off[u] + (int)lvl * CHUNK_EDGES;
+                re = min(g.off[u + 1], rb + CHUNK_EDGES);
+                lvl = (uint32_t)gcq::ld_rlx((const int*)&s->level[u]) + 1;
+                big = 1;
             } else {
                 ++n_items;
                 srv_slot* s = &x.slots[slot];
@@ -261,7 +277,20 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
                 } else {
                     const srv_graph& g = x.graphs[s->graph];
                     const int beg = g.off[v], end = g.off[v + 1];
-                    if (end - beg > WARP_DEG) {
+                    if (end - beg > HUB_DEG) {
+                        const uint32_t chunks = (uint32_t)((end - beg + CHUNK_EDGES - 1) / CHUNK_EDGES);
+                        if (chunks >= CLEANUP) {
+                            gcq::raise_error(&c->err, gcq::ERR_CAPACITY);
+                            settle(x, slot, 0, tid);
+                        } else {
+                            // the chunks inherit this item's count
+                            gcq::fetch_add(&s->pending, (uint64_t)chunks - 1);
+                            for (uint32_t k = 0; k < chunks; ++k) push_item(x, pack_item(slot, k, v | CHUNK_BIT), tid);
+                        }
+                    } else if (end - beg > WARP_DEG) {
+                        rb = beg;
+                        re = end;
+                        lvl = lvl + 1;
                         big = 1;
                     } else {
                         n_edges += (uint64_t)(end - beg);
@@ -293,12 +322,12 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
             const uint32_t os = __shfl_sync(FULL, slot, owner);
             const uint32_t ol = __shfl_sync(FULL, lvl, owner);
             const uint32_t ov = __shfl_sync(FULL, v, owner);
+            const int beg = __shfl_sync(FULL, rb, owner), end = __shfl_sync(FULL, re, owner);
             srv_slot* s = &x.slots[os];
             const srv_graph& g = x.graphs[s->graph];
             int32_t* level = s->level;
             if (kind == 1) {
-                const int beg = g.off[ov], end = g.off[ov + 1];
-                const uint32_t lv = ol + 1;
+                const uint32_t lv = ol;   // the level this range's neighbours get
                 if (lane == owner) n_edges += (uint64_t)(end - beg);
                 if (lv > MAX_LEVEL) {
                     if (lane == owner) gcq::raise_error(&c->err, gcq::ERR_CAPACITY);

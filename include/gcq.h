@@ -265,7 +265,9 @@ int gcq_bfs_destroy(gcq_bfs_ctx* c);
 /* One traversal from src (run_bfs, bfs_bench.cpp:509-633).  persistent = 0 launches
  * bfs_expand_kernel + bfs_hub_kernel per level and reads the next frontier size on
  * the host, as the reference does; persistent = 1 runs every level in one
- * cooperative launch with grid barriers.  host_levels (V entries, may be NULL)
+ * cooperative launch with grid barriers; persistent = 2 (G-WFQ, G-LFQ) runs an
+ * asynchronous label-correcting traversal in one launch with one queue and no
+ * level barrier (same depths; max_frontier is reported as 0).  host_levels (V entries, may be NULL)
  * receives the depths, -1 for unreached vertices.  A frontier larger than the queue
  * returns GCQ_ECAPACITY (the reference drops the vertices silently). */
 int gcq_bfs_run(gcq_bfs_ctx* c, int32_t src, uint32_t block, int persistent, int32_t* host_levels,

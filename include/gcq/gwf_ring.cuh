@@ -495,6 +495,23 @@ __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid
     enqueue(&q->fq, idx, tid);   // releases the slot only after the read above
     return true;
 }
+// Enqueue for workloads whose consumers poll (the reference has none): fast-path
+// attempts only.  With many pollers a request on the wait-free slow path does not
+// catch the dequeue front (its tickets come one CAS at a time while pollers take
+// Head tickets by the thousand), so this enqueue stays lock-free instead.  false
+// when no free index turns up in `tries` attempts (the queue is full); a full item
+// ring after GCQ_SPIN_LIMIT attempts sets ERR_SPIN.
+__device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t tid, uint32_t tries) {
+    const uint32_t idx = try_dequeue(&q->fq, tid, tries);
+    if (idx == BOT) return false;
+    st_rlx(&q->data[idx], value);
+    const cfg c = load_cfg(&q->aq);
+    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k)
+        if (try_enq(&q->aq, c, idx) == 0) return true;   // release CAS publishes data[idx]
+    raise_error(c.err, ERR_SPIN);
+    return false;
+}
+
 // try_dequeue on the item ring of an MPMC queue.
 __device__ __forceinline__ bool try_dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->aq, tid, tries);

@@ -92,3 +92,49 @@ def test_bfs_graph_a_gwfq(gcq, oracle_lib):
             r, lv = b.run(src=0, block=256, persistent=persistent)
             assert np.array_equal(lv, want)
             assert r["levels"] == int(want.max()) + 1
+
+
+# ------------------------------------------------------- asynchronous (persistent=2)
+@pytest.mark.parametrize("kind", ["gwfq", "glfq"])
+def test_bfs_async_graph_b_and_grid(gcq, oracle_lib, graph_b, kind):
+    """The label-correcting form gives the same depths, whatever the order."""
+    off, idx = graph_b
+    want = _serial(oracle_lib, off, idx)
+    with gcq.Bfs(kind, off, idx, threads=16384) as b:
+        for rep in range(3):
+            r, lv = b.run(src=0, block=256, persistent=2)
+            assert np.array_equal(lv, want)
+            assert r["reached"] == int((want >= 0).sum())
+            assert r["levels"] == int(want.max()) + 1
+    off, idx = gcq.graph_grid(64, 96, 1.0, 0.0, 0)
+    with gcq.Bfs(kind, off, idx, threads=2048) as b:
+        for src in [0, 17, 64 * 96 - 1]:
+            r, lv = b.run(src=src, block=256, persistent=2)
+            assert np.array_equal(lv, _serial(oracle_lib, off, idx, src))
+
+
+def test_bfs_async_hubs_and_rmat(gcq, oracle_lib):
+    off, idx = gcq.graph_rmat(14, 16, seed=9)      # skewed degrees: warp-wide expansion
+    want = _serial(oracle_lib, off, idx)
+    with gcq.Bfs("gwfq", off, idx, threads=65536) as b:
+        r, lv = b.run(src=0, block=256, persistent=2)
+        assert np.array_equal(lv, want)
+        assert r["edges_scanned"] >= int(np.diff(off)[want >= 0].sum())   # every reached vertex expanded
+
+
+def test_bfs_async_graph_a(gcq, oracle_lib):
+    off, idx = gcq.graph_grid(4096, 4096, 0.6, 0.01, SEED)
+    want = _serial(oracle_lib, off, idx)
+    with gcq.Bfs("gwfq", off, idx, threads=65536) as b:
+        r, lv = b.run(src=0, block=256, persistent=2)
+        assert np.array_equal(lv, want)
+        assert r["levels"] == int(want.max()) + 1
+
+
+@pytest.mark.parametrize("kind", ["sfq", "wfq"])
+def test_bfs_async_unsupported(gcq, graph_b, kind):
+    off, idx = graph_b
+    with gcq.Bfs(kind, off, idx, threads=512) as b:
+        with pytest.raises(gcq.GcqError) as e:
+            b.run(src=0, block=256, persistent=2)
+        assert e.value.status == gcq.EUNSUPPORTED
