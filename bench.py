@@ -126,6 +126,24 @@ def cpu_baseline(seconds=3.0, order=CAPACITY_LOG2):
                       % (cores, order, seconds)}
 
 
+def per_queue(g):
+    """Every queue of the sweep, balanced and split 50 %, at its largest thread count
+    within its envelope (gcq_tb_run, CUDA-graph chunks of 128 ops, 300 ms)."""
+    out = {}
+    for kind, cap, threads in [("gwfq", 20, 262144), ("glfq", 20, 262144), ("sfq", 16, 32768), ("wfq", 0, 65536)]:
+        row = {"threads": threads, "capacity_log2": cap}
+        for mode, name in [(0, "balanced"), (1, "split50")]:
+            t = threads if mode == 0 else min(threads, 65536)
+            with g.Queue(kind, cap, t) as q:
+                r = q.tb_run(mode=mode, producer_percent=50, threads=t, chunk_ops=128, warmup_ms=100, run_ms=300,
+                             graph_chunks=8)
+            row[name + "_mops"] = round(r["succ_mops"], 1)
+            if mode == 1:
+                row["split_threads"] = t
+        out[kind] = row
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -288,6 +306,8 @@ def run_gpu(args):
                         "max": round(max(step_ms), 4)},
             "counters": {"enq_success": c[0], "enq_fail": c[1], "deq_success": c[2], "deq_empty": c[3]},
         }
+        if not args.no_per_queue:
+            line["queues"] = per_queue(g)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         print(json.dumps(line), flush=True)
@@ -427,6 +447,7 @@ def main():
     ap.add_argument("--capacity-log2", type=int, default=CAPACITY_LOG2)
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-per-queue", action="store_true", help="skip the table of all four queues")
     ap.add_argument("--workload", choices=["tb", "served-bfs"], default="tb")
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--serve-rate", type=float, default=0.0, help="Poisson arrivals per second (0: closed batch)")

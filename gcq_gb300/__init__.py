@@ -88,6 +88,11 @@ SERVE_RES_DTYPE = np.dtype([("admit_ns", "<u8"), ("done_ns", "<u8"), ("finish_ns
                             ("checksum", "<u8"), ("reached", "<u4"), ("max_level", "<i4")])
 
 
+class TunePoint(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("chunk_ops", C.c_uint32), ("deq_wait", C.c_uint32), ("remap", C.c_uint32),
+                ("succ_mops", C.c_double), ("status", C.c_int32), ("_pad", C.c_int32)]
+
+
 class GcqError(RuntimeError):
     def __init__(self, status, what=""):
         self.status = status
@@ -131,6 +136,8 @@ SIGNATURES = {
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
     "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
+    "gcq_tb_autotune": ([I32, U32, U32, I32, I32, C.c_double, U32, C.POINTER(TunePoint), C.POINTER(TunePoint), SZ,
+                         C.POINTER(SZ)], I32),
     "gcq_serve_default_cfg": ([C.POINTER(ServeCfg)], None),
     "gcq_serve_create": ([I32, P, P, P, P, C.POINTER(ServeCfg), C.POINTER(P)], I32),
     "gcq_serve_destroy": ([P], I32),
@@ -293,6 +300,19 @@ class Queue:
         r = FifoResult()
         _check(_lib().gcq_fifo_check(self._h, threads, block, ops_per_thread, C.byref(r)), "gcq_fifo_check")
         return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+
+def autotune(kind: str, capacity_log2: int, threads: int, mode: int = 0, producer_percent: int = 50,
+             ms_per_point: float = 60.0, passes: int = 2) -> dict:
+    """Autotune block, chunk length and queue knobs of one throughput configuration
+    (gcq_tb_autotune); returns {"best": {...}, "table": [...]}."""
+    best = TunePoint()
+    table = (TunePoint * 256)()
+    n = SZ()
+    _check(_lib().gcq_tb_autotune(KINDS[kind], capacity_log2, threads, mode, producer_percent, ms_per_point, passes,
+                                  C.byref(best), table, 256, C.byref(n)), "gcq_tb_autotune")
+    row = lambda p: {f: getattr(p, f) for f, _ in TunePoint._fields_ if not f.startswith("_")}
+    return {"best": row(best), "table": [row(table[i]) for i in range(min(n.value, 256))]}
 
 
 def graph_grid(rows: int, cols: int, keep_p: float = 0.6, diag_p: float = 0.01, seed: int = 1):

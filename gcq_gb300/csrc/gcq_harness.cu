@@ -7,6 +7,10 @@
 #include <mutex>
 #include <vector>
 
+#include <map>
+#include <tuple>
+#include <vector>
+
 #include "gcq_internal.cuh"
 
 using gcqi::qops;
@@ -535,4 +539,107 @@ extern "C" int gcq_tb_chunk_host_noalloc(gcq_queue* q, int mode, int producer_pe
     GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
     GCQ_CUDA(cudaStreamSynchronize(s));
     return GCQ_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+// Coordinate descent over the launch shape and the queue knobs of one throughput
+// configuration (the reference fixes them at compile time and sweeps by hand:
+// throughout_bench.cpp:1088, Makefile TB_* knobs).  Each candidate is a fresh queue
+// and a short gcq_tb_run; a knob moves to the value with the highest successful
+// operation rate while the others stay at their current best, and the sweep makes
+// `passes` rounds over the knobs.
+namespace {
+
+struct tune_space {
+    std::vector<uint32_t> block, chunk, deq_wait, remap;
+};
+
+int tune_point(int kind, uint32_t capacity_log2, uint32_t threads, int mode, int pp, double ms,
+               const gcq_tune_point& p, double* mops) {
+    gcq_knobs k;
+    gcq_default_knobs(&k);
+    k.deq_wait = p.deq_wait;
+    k.remap = p.remap;
+    gcq_queue* q = nullptr;
+    int rc = gcq_create(kind, capacity_log2, threads, &k, &q);
+    if (rc != GCQ_OK) return rc;
+    gcq_tb_result r;
+    rc = gcq_tb_run(q, mode, pp, threads, p.block, p.chunk_ops, ms / 3, ms, 8, &r);
+    if (rc == GCQ_OK) {
+        uint32_t err = 0;
+        gcq_error_word(q, &err, 0);
+        if (err & ~GCQ_ERR_POOL) rc = GCQ_EDEVICE;
+    }
+    gcq_destroy(q);
+    if (rc != GCQ_OK) return rc;
+    *mops = r.gpu_ms > 0 ? (double)(r.counters.enq_success + r.counters.deq_success) / (r.gpu_ms * 1e3) : 0.0;
+    return GCQ_OK;
+}
+
+}  // namespace
+
+extern "C" int gcq_tb_autotune(int kind, uint32_t capacity_log2, uint32_t threads, int mode, int producer_percent,
+                               double ms_per_point, uint32_t passes, gcq_tune_point* best, gcq_tune_point* table,
+                               size_t cap, size_t* n_out) {
+    if (!best || threads == 0 || ms_per_point <= 0 || passes == 0) return GCQ_EINVAL;
+    tune_space sp;
+    sp.block = {128, 256, 512, 1024};
+    sp.chunk = {32, 64, 128, 256};
+    if (kind == GCQ_GWFQ || kind == GCQ_GLFQ) {
+        sp.deq_wait = {0, 2, 8, 32};
+        sp.remap = {0, 1};
+    } else {
+        sp.deq_wait = {8};
+        sp.remap = {0};
+    }
+    gcq_knobs dk;
+    gcq_default_knobs(&dk);
+    gcq_tune_point cur;
+    memset(&cur, 0, sizeof cur);
+    cur.block = 256;
+    cur.chunk_ops = 128;
+    cur.deq_wait = (kind == GCQ_GWFQ || kind == GCQ_GLFQ) ? dk.deq_wait : 8;
+    cur.remap = kind == GCQ_GLFQ ? 1u : 0u;
+    size_t n = 0;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, double> seen;
+    auto eval = [&](gcq_tune_point p) -> double {
+        const auto key = std::make_tuple(p.block, p.chunk_ops, p.deq_wait, p.remap);
+        auto it = seen.find(key);
+        if (it != seen.end()) return it->second;
+        double mops = -1.0;
+        if (threads % p.block == 0) {
+            const int rc = tune_point(kind, capacity_log2, threads, mode, producer_percent, ms_per_point, p, &mops);
+            if (rc == GCQ_ECUDA) return -2.0;   // the context may be unusable: stop
+            if (rc != GCQ_OK) mops = -1.0;
+        }
+        seen[key] = mops;
+        p.succ_mops = mops;
+        p.status = mops >= 0 ? 0 : -1;
+        if (table && n < cap) table[n] = p;
+        ++n;
+        return mops;
+    };
+    double best_v = eval(cur);
+    if (best_v == -2.0) return GCQ_ECUDA;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        for (int knob = 0; knob < 4; ++knob) {
+            const std::vector<uint32_t>& vals =
+                knob == 0 ? sp.block : knob == 1 ? sp.chunk : knob == 2 ? sp.deq_wait : sp.remap;
+            for (uint32_t v : vals) {
+                gcq_tune_point p = cur;
+                (knob == 0 ? p.block : knob == 1 ? p.chunk_ops : knob == 2 ? p.deq_wait : p.remap) = v;
+                const double m = eval(p);
+                if (m == -2.0) return GCQ_ECUDA;
+                if (m > best_v) {
+                    best_v = m;
+                    cur = p;
+                }
+            }
+        }
+    }
+    cur.succ_mops = best_v;
+    cur.status = best_v >= 0 ? 0 : -1;
+    *best = cur;
+    if (n_out) *n_out = n;
+    return best_v >= 0 ? GCQ_OK : GCQ_EDEVICE;
 }

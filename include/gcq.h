@@ -51,8 +51,9 @@ typedef struct gcq_knobs {
     uint32_t help_delay;          /* G-WFQ WF_HELP_DELAY, gwf_queue.hpp:296-298 (64) */
     uint32_t enq_patience;        /* G-WFQ WF_ENQ_PATIENCE, gwf_queue.hpp:300-302 (128) */
     uint32_t deq_patience;        /* G-WFQ WF_DEQ_PATIENCE, gwf_queue.hpp:304-306 (256) */
-    uint32_t remap;               /* slot permutation: 0 identity (G-WFQ default, gwf_ring.hpp:43-50),
-                                     1 spread tickets over 128-B lines (G-LFQ default, glf_queue.hpp:116-120) */
+    uint32_t remap;               /* slot permutation: 0 identity (the default for both rings here, as the
+                                     reference's G-WFQ, gwf_ring.hpp:43-50), 1 spread tickets over 128-B
+                                     lines (the reference's G-LFQ default, glf_queue.hpp:116-120) */
     uint32_t ymc_patience;        /* WF_PATIENCE, wfqueue_hip_opt.hpp:29-31 (16) */
     uint32_t ymc_ops_per_thread;  /* WF_PREALLOC_OPS_PER_THREAD, wfqueue_hip_opt.hpp:33-35 (512) */
     uint64_t wait_timeout_ns;     /* deadline of one blocking wait (SFQ), default 2 s */
@@ -202,6 +203,24 @@ int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, u
  * was called (logical clock); the reference's atomicMax order check (:585-588)
  * starts from 0xFFFFFFFF (:691) and never fires.  ops_per_thread is capped to
  * capacity / threads for bounded queues (:627-653); 0 after the cap = skipped. */
+/* Autotuner (no counterpart in the reference, which fixes these at compile time):
+ * coordinate descent over block {128..1024}, chunk_ops {32..256} and, for G-WFQ and
+ * G-LFQ, the deq_wait back-off {0, 2, 8, 32} and the slot permutation {0, 1}, each
+ * candidate a fresh queue of 2^capacity_log2 and a gcq_tb_run of ms_per_point;
+ * `passes` rounds over the knobs.  *best receives the fastest point; table (cap
+ * entries, may be NULL) every point measured, *n_out their number.  Blocks that do
+ * not divide `threads` are skipped (status -1). */
+typedef struct gcq_tune_point {
+    uint32_t block, chunk_ops, deq_wait, remap;
+    double succ_mops;      /* successful operations per microsecond (Mops/s) */
+    int32_t status;        /* 0 measured, -1 skipped or failed */
+    int32_t _pad;
+} gcq_tune_point;
+
+int gcq_tb_autotune(int kind, uint32_t capacity_log2, uint32_t threads, int mode, int producer_percent,
+                    double ms_per_point, uint32_t passes, gcq_tune_point* best, gcq_tune_point* table, size_t cap,
+                    size_t* n_out);
+
 typedef struct gcq_fifo_result {
     uint64_t in_count, out_count;
     uint32_t err_oob, err_dup, err_order, err_missing, err_gt1;

@@ -9,7 +9,8 @@
 // the enqueue CAS is tried first against the steady-state free slot, and a
 // dequeuer waits briefly for the enqueuer holding its ticket before marking the
 // slot (deq_wait);
-// the permutation spreads over 128-byte lines (16 entries) by default; Tail, Head
+// the slot permutation (128-byte lines, 16 entries) is a knob, identity by default
+// (with warp-aggregated tickets contiguous slots coalesce in L2); Tail, Head
 // and Threshold sit GCQ_HOT_STRIDE apart; loads are acquire/relaxed loads instead of
 // atomicAdd(p, 0) (:144-148); retry loops are bounded (GCQ_SPIN_LIMIT) and report
 // through the header's error word instead of spinning forever.
