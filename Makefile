@@ -8,6 +8,7 @@
 #   make bfs QUEUE=gwfq BFS_GEN="--grid 4096 4096 --keep 0.6 --diag 0.01 --seed 2"
 #   make bfs QUEUE=glfq BFS_GRAPH=graphs/road_usa.mtx
 #   make rt QUEUE=gwfq SCENE=1 THREADS=1024 BOUNCES=4
+#   make rt-compact SCENE=2 BOUNCES=12      (the stream-compaction baseline)
 #
 # The linearizability checker is test infrastructure here (oracle/), run by the
 # test suite rather than by a make target.
@@ -88,8 +89,8 @@ BFS_BIN := $(BFS_BUILD_DIR)/bfs_$(QUEUE)
 HXX = $(CXX) -O2 -std=c++17 -Iinclude -I$(HARNESS) $(QUEUE_DEF)
 HLINK = -L$(LIB_DIR) -lgcq -Wl,-rpath,$(abspath $(LIB_DIR)) -pthread
 
-.PHONY: all lib rt rt-build rt-run tb tb-build tb-run tb-build-fifo tb-run-fifo hist hist-build hist-run \
-        hist-run-all bfs bfs-build bfs-build-all bfs-run clean
+.PHONY: all lib rt rt-build rt-run rt-compact rt-compact-build rt-compact-run tb tb-build tb-run tb-build-fifo tb-run-fifo hist hist-build hist-run \
+        hist-run-all bfs bfs-build bfs-build-all bfs-run bfs-sweep clean
 
 all: rt
 
@@ -107,6 +108,16 @@ rt-build: lib
 rt-run: rt-build
 	@echo "[RT] Running $(RT_BIN) scene=$(SCENE) bounces=$(BOUNCES) threads=$(THREADS)"
 	GPU_NAME="$(GPU_NAME)" $(RT_BIN) $(SCENE) $(BOUNCES) $(THREADS)
+
+rt-compact: rt-compact-run
+
+rt-compact-build: lib
+	@mkdir -p $(RT_BUILD_DIR)
+	@echo "[RT] Building $(RT_BUILD_DIR)/rt_compact (stream-compaction baseline)"
+	$(HXX) $(EXTRA_FLAGS) $(HARNESS)/rt_compact.cpp -o $(RT_BUILD_DIR)/rt_compact $(HLINK)
+
+rt-compact-run: rt-compact-build
+	GPU_NAME="$(GPU_NAME)" $(RT_BUILD_DIR)/rt_compact $(SCENE) $(BOUNCES)
 
 tb: tb-run
 
@@ -174,6 +185,36 @@ bfs-run: bfs-build
 		$(if $(BFS_GEN),$(BFS_GEN),--graph "$(BFS_GRAPH)") \
 		--threads "$(BFS_THREADS)" --block "$(BFS_BLOCK)" --src "$(BFS_SRC_VERTEX)" \
 		--iters "$(BFS_ITERS)" --warmup "$(BFS_WARMUP)" --persistent "$(BFS_PERSISTENT)"
+
+# The sweep of concurrent_bfs/run_bfs_sweep.sh: every queue x thread count x graph,
+# one log per point, rows appended to BFS_CSV_NAME.  BFS_GRAPHS lists .mtx/SNAP files
+# (relative to BFS_GRAPH_DIR); left empty it sweeps the two generated grids.
+BFS_QUEUES ?= gwfq glfq wfq sfq
+BFS_CHUNKS ?= 512 1024 2048 4096 8192
+BFS_GRAPHS ?=
+BFS_LOG_DIR ?= out/bfs_logs
+BFS_GPU_FAMILY ?= gb300
+BFS_GEN_GRAPHS := gridA:--grid 4096 4096 --keep 0.6 --diag 0.01 --seed 2|gridB:--grid 212 212 --keep 0.6 --diag 0.01 --seed 2
+
+bfs-sweep: bfs-build-all
+	@mkdir -p $(BFS_LOG_DIR)
+	@set -e; \
+	if [ -n "$(BFS_GRAPHS)" ]; then \
+		specs=""; for g in $(BFS_GRAPHS); do \
+			case "$$g" in /*) p="$$g" ;; *) p="$(BFS_GRAPH_DIR)/$$g" ;; esac; \
+			specs="$$specs|$$(basename $$g):--graph $$p"; done; specs="$${specs#|}"; \
+	else specs="$(BFS_GEN_GRAPHS)"; fi; \
+	IFS='|'; for spec in $$specs; do \
+		name="$${spec%%:*}"; args="$${spec#*:}"; \
+		for q in $(BFS_QUEUES); do for t in $(BFS_CHUNKS); do \
+			log="$(BFS_LOG_DIR)/bfs_$${q}_$(BFS_GPU_FAMILY)_$${name}_$${t}.log"; \
+			echo "[BFS] $$q $$name threads=$$t -> $$log"; \
+			IFS=' '; CSV_NAME=$(BFS_CSV_NAME) GPU_NAME="$(GPU_NAME)" $(BFS_BUILD_DIR)/bfs_$$q $$args \
+				--threads $$t --block $(BFS_BLOCK) --src $(BFS_SRC_VERTEX) --iters $(BFS_ITERS) \
+				--warmup $(BFS_WARMUP) --persistent $(BFS_PERSISTENT) > "$$log" 2>&1 || echo "[BFS] failed, see $$log"; \
+			IFS='|'; \
+		done; done; \
+	done
 
 clean:
 	rm -rf out

@@ -136,6 +136,7 @@ SIGNATURES = {
     "gcq_bfs_destroy": ([P], I32),
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
     "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
+    "gcq_rt_compact_render": ([I32, I32, I32, I32, P, C.POINTER(RtResult)], I32),
     "gcq_tb_autotune": ([I32, U32, U32, I32, I32, C.c_double, U32, C.POINTER(TunePoint), C.POINTER(TunePoint), SZ,
                          C.POINTER(SZ)], I32),
     "gcq_serve_default_cfg": ([C.POINTER(ServeCfg)], None),
@@ -491,6 +492,15 @@ def rt_render(kind: str = "gwfq", scene: int = 0, width: int = 1280, height: int
     r = RtResult()
     _check(_lib().gcq_rt_render(KINDS[kind], scene, width, height, tiles_x, tiles_y, threads_per_tile,
                                 max_bounces, queue_log2, img.ctypes.data, C.byref(r)), "gcq_rt_render")
+    return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
+
+
+def rt_compact_render(scene: int = 0, width: int = 1280, height: int = 720, max_bounces: int = 4):
+    """Render one frame with the stream-compaction baseline; returns (result, image HxWx3)."""
+    img = np.zeros((height, width, 3), dtype=np.float32)
+    r = RtResult()
+    _check(_lib().gcq_rt_compact_render(scene, width, height, max_bounces, img.ctypes.data, C.byref(r)),
+           "gcq_rt_compact_render")
     return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
 
 

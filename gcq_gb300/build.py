@@ -26,9 +26,13 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(OUT, "libgcq.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
-# Per-file extra flags: the ray tracer's float math must round exactly like the
-# CPU reference render, so it is compiled without FMA contraction.
+# Host code is compiled without floating-point contraction as well: on Arm the host
+# compiler would otherwise fuse a*b+c in host-side setup (the ray tracer's scene),
+# which then differs in the last bit from the CPU oracle built the same way.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I" + INCLUDE, "-I" + CSRC]
+# Per-file extra flags: the ray tracer's device float math must round exactly like
+# the CPU reference render, so it is compiled without FMA contraction.
 EXTRA = {"gcq_rt.cu": ["--fmad=false"]}
 
 

@@ -274,6 +274,28 @@ void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, r
         sph.push_back({v3(0.0f, 1.3f, -5.5f), 1.3f, v3(.4f, .6f, .95f), 0.0f});
         P.cam_o = v3(0, 0.3f, 0.5f);
         P.cam_f = normalize(v3(0, -0.2f, -1.f));
+    } else if (scene == 2) {
+        // the compaction baseline's "mirror tunnel" (rt_compaction.cpp:554-592, camera
+        // :705-707): mirror walls, matte absorbers, a chain of near-perfect mirrors
+        for (const Plane& p : {Plane{v3(1, 0, 0), 2.0f, v3(.95f, .95f, .95f), 0.985f},
+                               Plane{v3(-1, 0, 0), 2.0f, v3(.95f, .95f, .95f), 0.985f},
+                               Plane{v3(0, 1, 0), 1.2f, v3(.95f, .95f, .95f), 0.985f},
+                               Plane{v3(0, -1, 0), 1.2f, v3(.95f, .95f, .95f), 0.985f},
+                               Plane{v3(0, 0, 1), 20.0f, v3(.95f, .95f, .95f), 0.985f},
+                               Plane{v3(0, 0, -1), 2.5f, v3(.95f, .95f, .95f), 0.985f}})
+            pln.push_back(p);
+        for (const Sphere& q : {Sphere{v3(-1.45f, -0.25f, -4.2f), 0.70f, v3(.85f, .20f, .20f), 0.00f},
+                                Sphere{v3(1.35f, 0.20f, -5.3f), 0.80f, v3(.20f, .85f, .25f), 0.00f},
+                                Sphere{v3(0.00f, -0.75f, -8.5f), 0.40f, v3(.85f, .85f, .20f), 0.00f},
+                                Sphere{v3(0.00f, 0.00f, -4.8f), 0.90f, v3(.95f, .95f, .95f), 0.995f},
+                                Sphere{v3(-0.75f, 0.35f, -7.2f), 0.85f, v3(.95f, .85f, .85f), 0.995f},
+                                Sphere{v3(0.80f, -0.25f, -9.8f), 0.90f, v3(.85f, .95f, .85f), 0.995f},
+                                Sphere{v3(-0.55f, 0.30f, -12.2f), 0.95f, v3(.85f, .85f, .95f), 0.995f},
+                                Sphere{v3(0.70f, -0.20f, -14.7f), 1.00f, v3(.95f, .95f, .80f), 0.995f},
+                                Sphere{v3(0.00f, 0.10f, -17.2f), 1.05f, v3(.90f, .90f, .95f), 0.995f}})
+            sph.push_back(q);
+        P.cam_o = v3(0.0f, 0.0f, 1.6f);
+        P.cam_f = normalize(v3(0.0f, 0.0f, -1.0f));
     } else {
         sph.push_back({v3(-0.6f, 0.5f, -2.5f), 0.5f, v3(.9f, .3f, .3f), 0.85f});
         sph.push_back({v3(0.6f, 0.6f, -2.8f), 0.6f, v3(.95f, .95f, .95f), 0.95f});
@@ -289,6 +311,130 @@ void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, r
     P.cam_u = normalize(v3(0, 1, 0));
 }
 
+// ------------------------------------------------ stream-compaction comparator
+// The double-buffer + stream-compaction renderer of concurrent_rt/baselines/
+// rt_compaction.cpp, the non-queue baseline: every pass traces the whole active
+// ray list, marks the rays that continue, and packs them in order (the reference's
+// Blelloch scan + scatter, :327-470) for the next pass.  Here a pass is three
+// launches with the counts kept on the device: the trace writes each warp's
+// continuation ballot and each block's count, one block scans the block counts,
+// and the scatter places each continuing ray at its block offset + warp prefix +
+// lane rank -- the same order an exclusive scan of the flags gives.
+struct CRay { V3 o, d; int pix, depth; };   // 32 bytes
+
+__global__ void k_cgen(CRay* __restrict__ rays, rt_params P) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= P.img_w * P.img_h) return;
+    const int px = idx % P.img_w, py = idx / P.img_w;
+    const float aspect = (float)P.img_w / (float)P.img_h;
+    const float u = ((px + 0.5f) / P.img_w - 0.5f) * 2.f * aspect;
+    const float v = -((py + 0.5f) / P.img_h - 0.5f) * 2.f;
+    CRay r;
+    r.o = P.cam_o;
+    r.d = normalize(add(P.cam_f, add(scale(P.cam_r, u), scale(P.cam_u, v))));   // :240-241
+    r.pix = idx;
+    r.depth = 0;
+    rays[idx] = r;
+}
+
+// kernel_trace_rays, rt_compaction.cpp:258-326, plus the flags and block counts
+__global__ void __launch_bounds__(256) k_ctrace(const CRay* __restrict__ in, const uint32_t* __restrict__ count,
+                                                CRay* __restrict__ tmp, uint32_t* __restrict__ masks,
+                                                uint32_t* __restrict__ block_cnt, const Sphere* __restrict__ sph,
+                                                int ns, const Plane* __restrict__ pln, int np,
+                                                float* __restrict__ img, int max_depth) {
+    const uint32_t n = *count;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    bool cont = false;
+    if (idx < n) {
+        const CRay r = in[idx];
+        const V3 light_dir = normalize(v3(-0.5f, 1.f, 0.2f));
+        const V3 ambient = v3(0.05f, 0.05f, 0.05f);
+        Ray q;
+        q.o = r.o;
+        q.d = r.d;
+        const Hit hit = trace_scene(q, sph, ns, pln, np);
+        V3 color;
+        if (hit.did_hit) {
+            const float NdotL = fmaxf(0.f, dot3(hit.n, light_dir));
+            color = add(ambient, scale(hit.albedo, NdotL));
+            if (hit.refl > 0.f && r.depth < max_depth) {
+                CRay o;
+                o.o = add(hit.p, scale(hit.n, 1e-4f));
+                o.d = normalize(reflect3(r.d, hit.n));
+                o.pix = r.pix;
+                o.depth = r.depth + 1;
+                tmp[idx] = o;
+                cont = true;
+            }
+        } else {
+            const float t = 0.5f * (r.d.y + 1.f);
+            color = add(scale(v3(1.f, 1.f, 1.f), 1.f - t), scale(v3(0.5f, 0.7f, 1.f), t));
+        }
+        color = scale(clamp01(color), r.depth == 0 ? 1.0f : 0.5f);
+        float* p = img + 3 * (size_t)r.pix;
+        // one ray per pixel per pass: the reference's atomicAdd is a plain add here
+        if (r.depth == 0) { p[0] = color.x; p[1] = color.y; p[2] = color.z; }
+        else { p[0] += color.x; p[1] += color.y; p[2] += color.z; }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, cont);
+    if ((threadIdx.x & 31) == 0) masks[idx >> 5] = m;
+    const int c = __syncthreads_count(cont);
+    if (threadIdx.x == 0) block_cnt[blockIdx.x] = (uint32_t)c;
+}
+
+// exclusive scan of the block counts in one block of 1024 threads; the total is
+// the next pass's ray count
+__global__ void __launch_bounds__(1024) k_cscan(const uint32_t* __restrict__ block_cnt, uint32_t nblocks,
+                                                uint32_t* __restrict__ block_off, uint32_t* __restrict__ total,
+                                                unsigned long long* __restrict__ traced, const uint32_t* __restrict__ count) {
+    __shared__ uint32_t warp_sum[32];
+    const uint32_t per = (nblocks + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t mine = 0;
+    for (uint32_t b = b0; b < b0 + per && b < nblocks; ++b) mine += block_cnt[b];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = mine;   // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_sum[lane] = w;
+    }
+    __syncthreads();
+    uint32_t run = (x - mine) + (warp > 0 ? warp_sum[warp - 1] : 0u);
+    for (uint32_t b = b0; b < b0 + per && b < nblocks; ++b) {
+        block_off[b] = run;
+        run += block_cnt[b];
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        *total = run;
+        atomicAdd(traced, (unsigned long long)*count);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cscatter(const CRay* __restrict__ tmp, const uint32_t* __restrict__ masks,
+                                                  const uint32_t* __restrict__ block_off, const uint32_t* __restrict__ count,
+                                                  CRay* __restrict__ out) {
+    __shared__ uint32_t wpre[8];
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t m = idx < *count ? masks[idx >> 5] : 0u;
+    if (lane == 0) wpre[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    uint32_t base = block_off[blockIdx.x];
+    for (int w = 0; w < warp; ++w) base += wpre[w];
+    if ((m >> lane) & 1u) out[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = tmp[idx];
+}
+
 }  // namespace
 
 extern "C" {
@@ -300,7 +446,7 @@ extern "C" {
 int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
                   int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out) {
     if (!out || width <= 0 || height <= 0 || tiles_x <= 0 || tiles_y <= 0 || threads_per_tile <= 0 ||
-        max_bounces < 0 || (scene != 0 && scene != 1) || queue_log2 < 4 || queue_log2 > 24)
+        max_bounces < 0 || scene < 0 || scene > 2 || queue_log2 < 4 || queue_log2 > 24)
         return GCQ_EINVAL;
     if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
     memset(out, 0, sizeof(*out));
@@ -467,6 +613,96 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
     return leftover ? GCQ_EDEVICE : GCQ_OK;
+}
+
+// Render one frame with the stream-compaction baseline (rt_compaction.cpp:593-897):
+// scenes 0, 1 and 2, every pass's rays packed in order for the next.  gen_ms is the
+// primary-ray launch, trace_ms the passes (trace + scan + scatter); total_rays sums
+// the rays of every pass, as the reference counts them.
+int gcq_rt_compact_render(int scene, int width, int height, int max_bounces, float* image, gcq_rt_result* out) {
+    if (!out || width <= 0 || height <= 0 || max_bounces < 0 || max_bounces > 64 || scene < 0 || scene > 2 ||
+        (uint64_t)width * height > (1u << 30))
+        return GCQ_EINVAL;
+    memset(out, 0, sizeof(*out));
+    rt_params P;
+    memset(&P, 0, sizeof P);
+    P.img_w = width;
+    P.img_h = height;
+    std::vector<Sphere> sph;
+    std::vector<Plane> pln;
+    build_scene(scene, sph, pln, P);
+    const uint32_t N = (uint32_t)width * height;
+    const uint32_t nblocks = (N + 255) / 256;
+    const int passes = max_bounces + 1;
+    CRay *d_a = nullptr, *d_b = nullptr, *d_t = nullptr;
+    uint32_t *d_masks = nullptr, *d_bcnt = nullptr, *d_boff = nullptr, *d_count = nullptr;
+    unsigned long long* d_traced = nullptr;
+    float* d_img = nullptr;
+    Sphere* d_sph = nullptr;
+    Plane* d_pln = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(d_a); cudaFree(d_b); cudaFree(d_t); cudaFree(d_masks); cudaFree(d_bcnt); cudaFree(d_boff);
+        cudaFree(d_count); cudaFree(d_traced); cudaFree(d_img); cudaFree(d_sph); cudaFree(d_pln);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (e2) cudaEventDestroy(e2);
+    };
+    const size_t rb = (size_t)N * sizeof(CRay);
+    if (cudaMalloc(&d_a, rb) != cudaSuccess || cudaMalloc(&d_b, rb) != cudaSuccess || cudaMalloc(&d_t, rb) != cudaSuccess ||
+        cudaMalloc(&d_masks, (size_t)nblocks * 8 * 4) != cudaSuccess ||
+        cudaMalloc(&d_bcnt, (size_t)nblocks * 4) != cudaSuccess || cudaMalloc(&d_boff, (size_t)nblocks * 4) != cudaSuccess ||
+        cudaMalloc(&d_count, (size_t)(passes + 1) * 4) != cudaSuccess || cudaMalloc(&d_traced, 8) != cudaSuccess ||
+        cudaMalloc(&d_img, (size_t)N * 12) != cudaSuccess ||
+        cudaMalloc(&d_sph, std::max<size_t>(1, sph.size()) * sizeof(Sphere)) != cudaSuccess ||
+        cudaMalloc(&d_pln, std::max<size_t>(1, pln.size()) * sizeof(Plane)) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return GCQ_ENOMEM;
+    }
+    auto fail = [&](cudaError_t e, const char* what) { cleanup(); return gcqi::cuda_fail(e, what, __FILE__, __LINE__); };
+    std::vector<uint32_t> hc(passes + 1, 0);
+    hc[0] = N;
+    cudaError_t ce = cudaMemcpy(d_count, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemset(d_traced, 0, 8);
+    if (ce == cudaSuccess) ce = cudaMemset(d_img, 0, (size_t)N * 12);
+    if (ce == cudaSuccess && !sph.empty()) ce = cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(Sphere), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !pln.empty()) ce = cudaMemcpy(d_pln, pln.data(), pln.size() * sizeof(Plane), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e2);
+    if (ce != cudaSuccess) return fail(ce, "rt compaction setup");
+    cudaEventRecord(e0);
+    k_cgen<<<nblocks, 256>>>(d_a, P);
+    cudaEventRecord(e1);
+    CRay* in = d_a;
+    CRay* outb = d_b;
+    for (int pass = 0; pass < passes; ++pass) {
+        k_ctrace<<<nblocks, 256>>>(in, d_count + pass, d_t, d_masks, d_bcnt, d_sph, (int)sph.size(), d_pln,
+                                   (int)pln.size(), d_img, max_bounces);
+        k_cscan<<<1, 1024>>>(d_bcnt, nblocks, d_boff, d_count + pass + 1, d_traced, d_count + pass);
+        if (pass + 1 < passes) k_cscatter<<<nblocks, 256>>>(d_t, d_masks, d_boff, d_count + pass, outb);
+        std::swap(in, outb);
+    }
+    cudaEventRecord(e2);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e2);
+    if (ce != cudaSuccess) return fail(ce, "rt compaction passes");
+    float gen_ms = 0, trace_ms = 0;
+    cudaEventElapsedTime(&gen_ms, e0, e1);
+    cudaEventElapsedTime(&trace_ms, e1, e2);
+    unsigned long long traced = 0;
+    ce = cudaMemcpy(&traced, d_traced, 8, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && image) ce = cudaMemcpy(image, d_img, (size_t)N * 12, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return fail(ce, "rt compaction results");
+    out->gen_ms = gen_ms;
+    out->trace_ms = trace_ms;
+    out->total_ms = gen_ms + trace_ms;
+    out->primary_rays = N;
+    out->total_rays = traced;
+    out->leftover = 0;
+    cleanup();
+    return GCQ_OK;
 }
 
 }  // extern "C"

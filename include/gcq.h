@@ -311,6 +311,14 @@ typedef struct gcq_rt_result {
 int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
                   int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out);
 
+/* The stream-compaction baseline (concurrent_rt/baselines/rt_compaction.cpp): the
+ * same scenes (plus its scene 2, the mirror tunnel, which gcq_rt_render also
+ * accepts), double-buffered ray lists packed in order after every pass, its own
+ * shading (each bounce weighted 0.5 and added; depth 0 written).  image (may be
+ * NULL) receives width*height RGB floats.  A non-queue comparator for the
+ * persistent per-tile tracer. */
+int gcq_rt_compact_render(int scene, int width, int height, int max_bounces, float* image, gcq_rt_result* out);
+
 /* ------------------------------------------------------------- roofline ----
  * The atomic roofline of this GPU, measured by a microbenchmark in the same
  * process (the reference reports raw Mops/s only).  Rates are operations per

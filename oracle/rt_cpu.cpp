@@ -71,13 +71,9 @@ Hit trace(const Ray& ray, const std::vector<Sphere>& sph, const std::vector<Plan
     return best;
 }
 
-}  // namespace
-
-// Renders into img (width*height*3 floats); returns the number of rays traced.
-extern "C" int64_t oracle_rt_render(int scene, int width, int height, int max_bounces, float* img) {
-    std::vector<Sphere> sph;
-    std::vector<Plane> pln;
-    F3 cam_o, cam_f;
+// Scenes 0 and 1 of rt_final.cpp:650-684 (identical in rt_compaction.cpp:501-552) with
+// their cameras (:849-859), and the compaction baseline's scene 2.
+void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, F3& cam_o, F3& cam_f) {
     if (scene == 0) {
         pln.push_back({f3(0, 1, 0), 1.f, f3(0.75f, 0.75f, 0.75f), 0.05f});
         const int gx = 10, gz = 10;
@@ -98,7 +94,7 @@ extern "C" int64_t oracle_rt_render(int scene, int width, int height, int max_bo
         sph.push_back({f3(0.0f, 1.3f, -5.5f), 1.3f, f3(.4f, .6f, .95f), 0.0f});
         cam_o = f3(0, 0.3f, 0.5f);
         cam_f = norm(f3(0, -0.2f, -1.f));
-    } else {
+    } else if (scene == 1) {
         sph.push_back({f3(-0.6f, 0.5f, -2.5f), 0.5f, f3(.9f, .3f, .3f), 0.85f});
         sph.push_back({f3(0.6f, 0.6f, -2.8f), 0.6f, f3(.95f, .95f, .95f), 0.95f});
         pln.push_back({f3(0, 1, 0), 1.f, f3(.9f, .9f, .9f), 0.3f});
@@ -108,7 +104,38 @@ extern "C" int64_t oracle_rt_render(int scene, int width, int height, int max_bo
         pln.push_back({f3(0, -1, 0), 2.5f, f3(.95f, .95f, .95f), 0.2f});
         cam_o = f3(0, 0.5f, 1.5f);
         cam_f = norm(f3(0, -0.1f, -1.f));
+    } else {
+        // mirror tunnel (rt_compaction.cpp:554-592): reflective walls, matte absorbers,
+        // a chain of near-perfect mirrors; camera :705-707
+        pln.push_back({f3(1, 0, 0), 2.0f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        pln.push_back({f3(-1, 0, 0), 2.0f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        pln.push_back({f3(0, 1, 0), 1.2f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        pln.push_back({f3(0, -1, 0), 1.2f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        pln.push_back({f3(0, 0, 1), 20.0f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        pln.push_back({f3(0, 0, -1), 2.5f, f3(0.95f, 0.95f, 0.95f), 0.985f});
+        sph.push_back({f3(-1.45f, -0.25f, -4.2f), 0.70f, f3(0.85f, 0.20f, 0.20f), 0.00f});
+        sph.push_back({f3(1.35f, 0.20f, -5.3f), 0.80f, f3(0.20f, 0.85f, 0.25f), 0.00f});
+        sph.push_back({f3(0.00f, -0.75f, -8.5f), 0.40f, f3(0.85f, 0.85f, 0.20f), 0.00f});
+        sph.push_back({f3(0.00f, 0.00f, -4.8f), 0.90f, f3(0.95f, 0.95f, 0.95f), 0.995f});
+        sph.push_back({f3(-0.75f, 0.35f, -7.2f), 0.85f, f3(0.95f, 0.85f, 0.85f), 0.995f});
+        sph.push_back({f3(0.80f, -0.25f, -9.8f), 0.90f, f3(0.85f, 0.95f, 0.85f), 0.995f});
+        sph.push_back({f3(-0.55f, 0.30f, -12.2f), 0.95f, f3(0.85f, 0.85f, 0.95f), 0.995f});
+        sph.push_back({f3(0.70f, -0.20f, -14.7f), 1.00f, f3(0.95f, 0.95f, 0.80f), 0.995f});
+        sph.push_back({f3(0.00f, 0.10f, -17.2f), 1.05f, f3(0.90f, 0.90f, 0.95f), 0.995f});
+        cam_o = f3(0.0f, 0.0f, 1.6f);
+        cam_f = norm(f3(0.0f, 0.0f, -1.0f));
     }
+
+}
+
+}  // namespace
+
+// Renders into img (width*height*3 floats); returns the number of rays traced.
+extern "C" int64_t oracle_rt_render(int scene, int width, int height, int max_bounces, float* img) {
+    std::vector<Sphere> sph;
+    std::vector<Plane> pln;
+    F3 cam_o, cam_f;
+    build_scene(scene, sph, pln, cam_o, cam_f);
     const F3 cam_r = norm(f3(1, 0, 0)), cam_u = norm(f3(0, 1, 0));
     const F3 light_dir = norm(f3(-0.5f, 1.f, 0.2f));
     const F3 ambient = f3(0.05f, 0.05f, 0.05f);
@@ -153,6 +180,62 @@ extern "C" int64_t oracle_rt_render(int scene, int width, int height, int max_bo
                     pix[0] += c.x; pix[1] += c.y; pix[2] += c.z;
                 }
                 break;
+            }
+        }
+    return traced;
+}
+
+// The double-buffer + stream-compaction baseline (concurrent_rt/baselines/
+// rt_compaction.cpp): primary rays as its kernel_generate_rays (:219-250, direction
+// f + (r*u + up*v)), and per bounce the shading of kernel_trace_rays (:258-326): a
+// hit gives ambient + albedo * max(0, N.L), a miss the sky gradient; the colour is
+// clamped to [0,1] and weighted 1.0 at depth 0 (written) and 0.5 after (added); a
+// surface with reflectivity > 0 continues the ray while depth < max_bounces.
+extern "C" int64_t oracle_rt_compact_render(int scene, int width, int height, int max_bounces, float* img) {
+    std::vector<Sphere> sph;
+    std::vector<Plane> pln;
+    F3 cam_o, cam_f;
+    build_scene(scene, sph, pln, cam_o, cam_f);
+    const F3 cam_r = norm(f3(1, 0, 0)), cam_u = norm(f3(0, 1, 0));
+    const F3 light_dir = norm(f3(-0.5f, 1.f, 0.2f));
+    const F3 ambient = f3(0.05f, 0.05f, 0.05f);
+    const float aspect = (float)width / (float)height;
+    std::memset(img, 0, sizeof(float) * 3 * (size_t)width * height);
+    int64_t traced = 0;
+    for (int py = 0; py < height; ++py)
+        for (int px = 0; px < width; ++px) {
+            const float u = ((px + 0.5f) / width - 0.5f) * 2.f * aspect;
+            const float v = -((py + 0.5f) / height - 0.5f) * 2.f;
+            Ray r;
+            r.o = cam_o;
+            r.d = norm(cam_f + (cam_r * u + cam_u * v));
+            r.depth = 0;
+            float* pix = img + 3 * ((size_t)py * width + px);
+            for (;;) {
+                ++traced;
+                const Hit hit = trace(r, sph, pln);
+                F3 color;
+                bool cont = false;
+                Ray refl;
+                if (hit.did_hit) {
+                    const float NdotL = fmaxf(0.f, dot(hit.n, light_dir));
+                    color = ambient + hit.albedo * NdotL;
+                    if (hit.refl > 0.f && r.depth < max_bounces) {
+                        refl.o = hit.p + hit.n * 1e-4f;
+                        refl.d = norm(reflect(r.d, hit.n));
+                        refl.depth = r.depth + 1;
+                        cont = true;
+                    }
+                } else {
+                    const float t = 0.5f * (r.d.y + 1.f);
+                    color = f3(1, 1, 1) * (1.f - t) + f3(0.5f, 0.7f, 1.f) * t;
+                }
+                const float w = r.depth == 0 ? 1.0f : 0.5f;
+                color = clamp01(color) * w;
+                if (r.depth == 0) { pix[0] = color.x; pix[1] = color.y; pix[2] = color.z; }
+                else { pix[0] += color.x; pix[1] += color.y; pix[2] += color.z; }
+                if (!cont) break;
+                r = refl;
             }
         }
     return traced;

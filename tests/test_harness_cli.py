@@ -35,7 +35,7 @@ def _compile(name, out, defines):
 
 
 def test_harness_binaries_built(built):
-    for exe in ["tb", "history", "bfs", "rt"]:
+    for exe in ["tb", "history", "bfs", "rt", "rt_compact"]:
         assert os.access(os.path.join(built, exe), os.X_OK), exe
 
 
@@ -125,3 +125,17 @@ def test_rt_cli_writes_image(built, oracle_lib, tmp_path):
     got = np.frombuffer(data[len(b"P6\n1280 720\n255\n"):], np.uint8).reshape(720, 1280, 3)
     assert np.array_equal(got, want)
     assert "GWFQ,cornell,256,4," in open(tmp_path / "rt_queue_perf.csv").read()
+
+
+@pytest.mark.gpu
+def test_rt_compact_cli(built, oracle_lib, tmp_path):
+    r = _run([os.path.join(built, "rt_compact"), "2", "6"], cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "Image saved: rt_COMPACT_mirror_tunnel.ppm" in r.stdout
+    img = np.zeros((720, 1280, 3), np.float32)
+    n = oracle_lib.lib().oracle_rt_compact_render(2, 1280, 720, 6, img.ctypes.data)
+    assert "Total rays traced: %d" % n in r.stdout
+    data = open(tmp_path / "rt_COMPACT_mirror_tunnel.ppm", "rb").read()
+    got = np.frombuffer(data[len(b"P6\n1280 720\n255\n"):], np.uint8).reshape(720, 1280, 3)
+    assert np.array_equal(got, np.clip(img * 255.0, 0, 255).astype(np.uint8))
+    assert ",COMPACT,256,%d," % n in open(tmp_path / "rt_performance.csv").read()
