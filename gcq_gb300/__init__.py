@@ -137,6 +137,7 @@ SIGNATURES = {
     "gcq_bfs_run": ([P, C.c_int32, U32, I32, P, C.POINTER(BfsResult)], I32),
     "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
     "gcq_rt_compact_render": ([I32, I32, I32, I32, P, C.POINTER(RtResult)], I32),
+    "gcq_rt_bounce_render": ([I32, I32, I32, I32, I32, I32, I32, U32, U64, P, C.POINTER(RtResult)], I32),
     "gcq_tb_autotune": ([I32, U32, U32, I32, I32, C.c_double, U32, C.POINTER(TunePoint), C.POINTER(TunePoint), SZ,
                          C.POINTER(SZ)], I32),
     "gcq_serve_default_cfg": ([C.POINTER(ServeCfg)], None),
@@ -492,6 +493,16 @@ def rt_render(kind: str = "gwfq", scene: int = 0, width: int = 1280, height: int
     r = RtResult()
     _check(_lib().gcq_rt_render(KINDS[kind], scene, width, height, tiles_x, tiles_y, threads_per_tile,
                                 max_bounces, queue_log2, img.ctypes.data, C.byref(r)), "gcq_rt_render")
+    return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
+
+
+def rt_bounce_render(kind: str = "gwfq", scene: int = 0, width: int = 1024, height: int = 1024, tile_px: int = 32,
+                     threads_per_tile: int = 1024, max_bounces: int = 4, queue_log2: int = 15, seed: int = 1):
+    """Render a benchmark scene (gcq_rt_bounce_render); returns (result, image HxWx3)."""
+    img = np.zeros((height, width, 3), dtype=np.float32)
+    r = RtResult()
+    _check(_lib().gcq_rt_bounce_render(KINDS[kind], scene, width, height, tile_px, threads_per_tile, max_bounces,
+                                       queue_log2, seed, img.ctypes.data, C.byref(r)), "gcq_rt_bounce_render")
     return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
 
 

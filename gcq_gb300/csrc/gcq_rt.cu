@@ -311,6 +311,431 @@ void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, r
     P.cam_u = normalize(v3(0, 1, 0));
 }
 
+
+
+// ------------------------------------------------ benchmark scenes, 1 sample/pixel
+// The ray-tracing workload of the benchmark configuration (the reference has no
+// such scenes; its two scenes are above): 1024x1024 pixels in 32x32-pixel tiles,
+// one sample per pixel, 32-byte rays (origin, direction, pixel id, depth) in the
+// per-tile ray-bounce queues.  Scene 0: 512 seeded spheres (60 % diffuse, 30 % metal,
+// 10 % glass) over a 40 x 40 ground quad under a sky.  Scene 1: a box room of five
+// diffuse quads, two axis-aligned boxes and an emitting ceiling quad.  A path
+// scatters per material (Lambertian, fuzzy metal, glass with Schlick reflectance)
+// until it leaves the scene, reaches the light, is absorbed or uses up max_bounces;
+// a pixel's one path contributes once, so the image needs no float atomics.
+// Sampling uses no transcendental function (PCG integers, rejection sampling,
+// Schlick as products), so the render is bit-identical to its CPU restatement.
+struct BRay { V3 o, d; uint32_t pix, depth; };   // 32 bytes
+struct BPix { V3 tp; uint32_t rng; };            // path throughput and RNG state, per pixel
+enum { B_DIFFUSE = 0, B_METAL = 1, B_GLASS = 2, B_LIGHT = 3 };
+struct BSphere { V3 c; float r; V3 albedo; float param; int mat; int _p[3]; };   // param: fuzz or index
+struct BQuad { int axis; float k, a0, a1, b0, b1; V3 albedo; int mat; };          // axis-aligned rectangle
+struct BCam { V3 o, lower_left, horiz, vert; };
+struct BHit { float t; V3 p, n; V3 albedo; float param; int mat; bool front, did_hit; };
+struct bparams {
+    int img_w, img_h, tiles_x, tile_w, tile_h, threads_per_tile, max_depth, sky;
+    BCam cam;
+    uint64_t seed, timeout_ns;
+};
+
+__host__ __device__ __forceinline__ float comp(V3 v, int i) { return i == 0 ? v.x : i == 1 ? v.y : v.z; }
+__host__ __device__ __forceinline__ uint32_t pcg_next(uint32_t& s) {
+    s = s * 747796405u + 2891336453u;
+    const uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+__host__ __device__ __forceinline__ float rand01(uint32_t& s) { return (float)(pcg_next(s) >> 8) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ V3 rand_in_unit_sphere(uint32_t& s) {
+    for (int k = 0; k < 64; ++k) {
+        const float x = 2.f * rand01(s) - 1.f;
+        const float y = 2.f * rand01(s) - 1.f;
+        const float z = 2.f * rand01(s) - 1.f;
+        const V3 p = v3(x, y, z);
+        if (dot3(p, p) < 1.f) return p;
+    }
+    return v3(0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ bool bhit_sphere(const BRay& r, const BSphere& sp, float tmax, BHit& h) {
+    const V3 oc = sub(r.o, sp.c);
+    const float a = dot3(r.d, r.d);
+    const float half_b = dot3(oc, r.d);
+    const float c = dot3(oc, oc) - sp.r * sp.r;
+    const float disc = half_b * half_b - a * c;
+    if (disc < 0.f) return false;
+    const float sq = sqrtf(disc);
+    float root = (-half_b - sq) / a;
+    if (root <= 1e-3f || root >= tmax) {
+        root = (-half_b + sq) / a;
+        if (root <= 1e-3f || root >= tmax) return false;
+    }
+    h.t = root;
+    h.p = add(r.o, scale(r.d, root));
+    const V3 outward = scale(sub(h.p, sp.c), 1.f / sp.r);
+    h.front = dot3(r.d, outward) < 0.f;
+    h.n = h.front ? outward : scale(outward, -1.f);
+    h.albedo = sp.albedo;
+    h.param = sp.param;
+    h.mat = sp.mat;
+    h.did_hit = true;
+    return true;
+}
+__device__ __forceinline__ bool bhit_quad(const BRay& r, const BQuad& q, float tmax, BHit& h) {
+    const float da = comp(r.d, q.axis);
+    if (fabsf(da) < 1e-8f) return false;
+    const float t = (q.k - comp(r.o, q.axis)) / da;
+    if (t <= 1e-3f || t >= tmax) return false;
+    const V3 p = add(r.o, scale(r.d, t));
+    const float u = q.axis == 0 ? p.y : p.x;
+    const float w = q.axis == 2 ? p.y : p.z;
+    if (u < q.a0 || u > q.a1 || w < q.b0 || w > q.b1) return false;
+    h.t = t;
+    h.p = p;
+    const V3 outward = v3(q.axis == 0 ? 1.f : 0.f, q.axis == 1 ? 1.f : 0.f, q.axis == 2 ? 1.f : 0.f);
+    h.front = da < 0.f;
+    h.n = h.front ? outward : scale(outward, -1.f);
+    h.albedo = q.albedo;
+    h.param = 0.f;
+    h.mat = q.mat;
+    h.did_hit = true;
+    return true;
+}
+__device__ __forceinline__ BHit btrace(const BRay& r, const BSphere* sph, int ns, const BQuad* quad, int nq) {
+    BHit best;
+    best.did_hit = false;
+    best.t = 1e30f;
+    for (int i = 0; i < ns; ++i) {
+        BHit h;
+        if (bhit_sphere(r, sph[i], best.t, h)) best = h;
+    }
+    for (int i = 0; i < nq; ++i) {
+        BHit h;
+        if (bhit_quad(r, quad[i], best.t, h)) best = h;
+    }
+    return best;
+}
+
+// One bounce of a path: true with r and st updated when the path continues; false
+// with *contrib set when it ends.
+__device__ __forceinline__ bool bshade(BRay& r, BPix& st, const BHit& hit, const bparams& P, V3* contrib) {
+    if (!hit.did_hit) {
+        if (P.sky) {
+            const V3 unit = normalize(r.d);
+            const float t = 0.5f * (unit.y + 1.f);
+            const V3 sky = add(scale(v3(1.f, 1.f, 1.f), 1.f - t), scale(v3(0.5f, 0.7f, 1.f), t));
+            *contrib = mulv(st.tp, sky);
+        } else {
+            *contrib = v3(0.f, 0.f, 0.f);
+        }
+        return false;
+    }
+    if (hit.mat == B_LIGHT) {
+        *contrib = mulv(st.tp, hit.albedo);
+        return false;
+    }
+    if ((int)r.depth >= P.max_depth) {
+        *contrib = v3(0.f, 0.f, 0.f);
+        return false;
+    }
+    V3 dir;
+    V3 att = hit.albedo;
+    if (hit.mat == B_DIFFUSE) {
+        dir = add(hit.n, normalize(rand_in_unit_sphere(st.rng)));
+        if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = hit.n;
+    } else if (hit.mat == B_METAL) {
+        const V3 refl = reflect3(normalize(r.d), hit.n);
+        dir = add(refl, scale(rand_in_unit_sphere(st.rng), hit.param));
+        if (dot3(dir, hit.n) <= 0.f) {
+            *contrib = v3(0.f, 0.f, 0.f);
+            return false;
+        }
+    } else {
+        const float ratio = hit.front ? 1.f / hit.param : hit.param;
+        const V3 unit = normalize(r.d);
+        const float cos_t = fminf(dot3(scale(unit, -1.f), hit.n), 1.f);
+        const float sin_t = sqrtf(1.f - cos_t * cos_t);
+        float r0 = (1.f - ratio) / (1.f + ratio);
+        r0 = r0 * r0;
+        const float x = 1.f - cos_t;
+        const float schlick = r0 + (1.f - r0) * (x * x * x * x * x);
+        const float u = rand01(st.rng);
+        if (ratio * sin_t > 1.f || schlick > u) {
+            dir = reflect3(unit, hit.n);
+        } else {
+            const V3 perp = scale(add(unit, scale(hit.n, cos_t)), ratio);
+            const V3 par = scale(hit.n, -sqrtf(fabsf(1.f - dot3(perp, perp))));
+            dir = add(perp, par);
+        }
+        att = v3(1.f, 1.f, 1.f);
+    }
+    r.o = hit.p;
+    r.d = normalize(dir);
+    r.depth += 1;
+    st.tp = mulv(st.tp, att);
+    return true;
+}
+
+// primary rays of a tile into its queue (as k_generate)
+template <int K>
+__global__ void k_bgen(char* rings, size_t stride, BRay* __restrict__ rays, BPix* __restrict__ pix, bparams P,
+                       unsigned long long* __restrict__ alive) {
+    const int tile = (int)blockIdx.y;
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (tid >= P.threads_per_tile) return;
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
+    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
+    const int tw = min(P.tile_w, P.img_w - x0), th = min(P.tile_h, P.img_h - y0);
+    int enqueued = 0;
+    for (int i = tid; i < tw * th; i += P.threads_per_tile) {
+        const int px = x0 + i % tw, py = y0 + i / tw;
+        const uint32_t g = (uint32_t)(py * P.img_w + px);
+        const float s = ((float)px + 0.5f) / (float)P.img_w;
+        const float t = 1.0f - ((float)py + 0.5f) / (float)P.img_h;
+        BRay r;
+        r.o = P.cam.o;
+        r.d = normalize(sub(add(add(P.cam.lower_left, scale(P.cam.horiz, s)), scale(P.cam.vert, t)), P.cam.o));
+        r.pix = g;
+        r.depth = 0;
+        BPix st;
+        st.tp = v3(1.f, 1.f, 1.f);
+        st.rng = (uint32_t)gcqi::splitmix64(P.seed ^ ((uint64_t)g << 20)) | 1u;
+        rays[g] = r;
+        pix[g] = st;
+        if (rtq<K>::enq(q, (uint32_t)i, (uint32_t)tid)) ++enqueued;   // release publishes the ray
+    }
+    if (enqueued > 0) atomicAdd(&alive[tile], (unsigned long long)enqueued);
+}
+
+template <int K>
+__global__ void k_btrace(char* rings, size_t stride, const BSphere* __restrict__ sph, int ns,
+                         const BQuad* __restrict__ quad, int nq, BRay* __restrict__ rays, BPix* __restrict__ pix,
+                         float* __restrict__ img, bparams P, unsigned long long* __restrict__ alive,
+                         unsigned long long* __restrict__ traced, gcq::u32a* err) {
+    const int tile = (int)blockIdx.y;
+    const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (tid >= P.threads_per_tile) return;
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
+    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
+    const int tw = min(P.tile_w, P.img_w - x0);
+    unsigned long long local_traced = 0;
+    gcq::backoff bo;
+    uint64_t last_progress = gcq::globaltimer_ns();
+    for (uint32_t it = 0;; ++it) {
+        if (gcq::ld_rlx((const gcq::u64a*)&alive[tile]) == 0) break;
+        uint32_t li;
+        if (!rtq<K>::deq(q, &li, (uint32_t)tid)) {
+            if ((it & 63) == 0 && gcq::globaltimer_ns() - last_progress > P.timeout_ns) {
+                gcq::raise_error(err, gcq::ERR_TIMEOUT);
+                break;
+            }
+            bo.pause(1024);
+            continue;
+        }
+        bo = gcq::backoff();
+        last_progress = gcq::globaltimer_ns();
+        const uint32_t g = (uint32_t)((y0 + (int)li / tw) * P.img_w + (x0 + (int)li % tw));
+        BRay r = rays[g];
+        BPix st = pix[g];
+        const BHit hit = btrace(r, sph, ns, quad, nq);
+        ++local_traced;
+        V3 c;
+        if (bshade(r, st, hit, P, &c)) {
+            rays[g] = r;
+            pix[g] = st;
+            if (!rtq<K>::enq(q, li, (uint32_t)tid)) atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+        } else {
+            float* o = img + 3 * (size_t)g;
+            o[0] = c.x; o[1] = c.y; o[2] = c.z;
+            atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+        }
+    }
+    if (local_traced > 0) atomicAdd(&traced[tile], local_traced);
+}
+
+uint64_t bscene_rand(uint64_t& s) {
+    s += 0x9e3779b97f4a7c15ULL;
+    return gcqi::splitmix64(s - 0x9e3779b97f4a7c15ULL);
+}
+float bscene_u01(uint64_t& s) { return (float)(bscene_rand(s) >> 40) * (1.0f / 16777216.0f); }
+
+BCam make_bcam(V3 from, V3 at, float half_h, float aspect) {
+    const V3 w = normalize(sub(from, at));
+    const V3 vup = v3(0.f, 1.f, 0.f);
+    const V3 u = normalize(v3(vup.y * w.z - vup.z * w.y, vup.z * w.x - vup.x * w.z, vup.x * w.y - vup.y * w.x));
+    const V3 v = v3(w.y * u.z - w.z * u.y, w.z * u.x - w.x * u.z, w.x * u.y - w.y * u.x);
+    BCam c;
+    c.o = from;
+    c.horiz = scale(u, 2.f * half_h * aspect);
+    c.vert = scale(v, 2.f * half_h);
+    c.lower_left = sub(sub(sub(from, scale(c.horiz, 0.5f)), scale(c.vert, 0.5f)), w);
+    return c;
+}
+
+void add_box(std::vector<BQuad>& q, V3 lo, V3 hi, V3 albedo) {
+    q.push_back({0, lo.x, lo.y, hi.y, lo.z, hi.z, albedo, B_DIFFUSE});
+    q.push_back({0, hi.x, lo.y, hi.y, lo.z, hi.z, albedo, B_DIFFUSE});
+    q.push_back({1, lo.y, lo.x, hi.x, lo.z, hi.z, albedo, B_DIFFUSE});
+    q.push_back({1, hi.y, lo.x, hi.x, lo.z, hi.z, albedo, B_DIFFUSE});
+    q.push_back({2, lo.z, lo.x, hi.x, lo.y, hi.y, albedo, B_DIFFUSE});
+    q.push_back({2, hi.z, lo.x, hi.x, lo.y, hi.y, albedo, B_DIFFUSE});
+}
+
+void build_bscene(int scene, uint64_t seed, std::vector<BSphere>& sph, std::vector<BQuad>& quad, bparams& P) {
+    const float aspect = (float)P.img_w / (float)P.img_h;
+    if (scene == 0) {
+        quad.push_back({1, 0.f, -20.f, 20.f, -20.f, 20.f, v3(0.5f, 0.5f, 0.5f), B_DIFFUSE});
+        uint64_t s = seed;
+        for (int i = 0; i < 512; ++i) {
+            const float r = 0.2f + 0.8f * bscene_u01(s);
+            const float x = -20.f + 40.f * bscene_u01(s);
+            const float z = -20.f + 40.f * bscene_u01(s);
+            const float m = bscene_u01(s);
+            BSphere b;
+            memset(&b, 0, sizeof b);
+            b.c = v3(x, r, z);
+            b.r = r;
+            if (m < 0.6f) {
+                const float a0 = bscene_u01(s), a1 = bscene_u01(s), a2 = bscene_u01(s);
+                b.albedo = v3(a0 * a0, a1 * a1, a2 * a2);
+                b.mat = B_DIFFUSE;
+            } else if (m < 0.9f) {
+                const float a0 = bscene_u01(s), a1 = bscene_u01(s), a2 = bscene_u01(s), f = bscene_u01(s);
+                b.albedo = v3(0.5f + 0.5f * a0, 0.5f + 0.5f * a1, 0.5f + 0.5f * a2);
+                b.param = 0.5f * f;
+                b.mat = B_METAL;
+            } else {
+                b.albedo = v3(1.f, 1.f, 1.f);
+                b.param = 1.5f;
+                b.mat = B_GLASS;
+            }
+            sph.push_back(b);
+        }
+        P.sky = 1;
+        P.cam = make_bcam(v3(13.f, 2.f, 3.f), v3(0.f, 0.f, 0.f), 0.17632698f /* tan 10 deg */, aspect);
+    } else {
+        const V3 white = v3(0.73f, 0.73f, 0.73f);
+        quad.push_back({1, 0.f, -1.f, 1.f, -1.f, 1.f, white, B_DIFFUSE});                           // floor
+        quad.push_back({1, 2.f, -1.f, 1.f, -1.f, 1.f, white, B_DIFFUSE});                           // ceiling
+        quad.push_back({2, -1.f, -1.f, 1.f, 0.f, 2.f, white, B_DIFFUSE});                           // back
+        quad.push_back({0, -1.f, 0.f, 2.f, -1.f, 1.f, v3(0.65f, 0.05f, 0.05f), B_DIFFUSE});         // left
+        quad.push_back({0, 1.f, 0.f, 2.f, -1.f, 1.f, v3(0.12f, 0.45f, 0.15f), B_DIFFUSE});          // right
+        quad.push_back({1, 1.999f, -0.3f, 0.3f, -0.3f, 0.3f, v3(15.f, 15.f, 15.f), B_LIGHT});      // light
+        add_box(quad, v3(-0.6f, 0.f, -0.6f), v3(-0.1f, 1.2f, -0.1f), white);
+        add_box(quad, v3(0.15f, 0.f, 0.f), v3(0.65f, 0.6f, 0.5f), white);
+        P.sky = 0;
+        P.cam = make_bcam(v3(0.f, 1.f, 3.4f), v3(0.f, 1.f, 0.f), 0.36397023f /* tan 20 deg */, aspect);
+    }
+}
+
+// ---------------------------------------------------------------- per-tile rings
+// One allocation holding a ring header per tile (stride apart) and each tile's
+// arrays, initialised for kind with threads_per_tile thread indices: the reference
+// allocates and initialises one queue per tile (rt_final.cpp:794-833).
+struct tile_rings {
+    char* dq = nullptr;
+    size_t stride = 0;
+    gcq::u32a* err = nullptr;
+};
+
+void free_tile_rings(tile_rings* tr) {
+    cudaFree(tr->dq);
+    tr->dq = nullptr;
+}
+
+int make_tile_rings(int kind, int tiles, int threads_per_tile, uint32_t queue_log2, uint64_t timeout_ns,
+                    tile_rings* tr) {
+    const uint64_t n = 1ull << queue_log2;
+    size_t stride = 0, per_tile = 0;
+    int bits = 5;
+    if (kind == GCQ_GWFQ) {
+        if ((uint64_t)threads_per_tile > n) return GCQ_EUNSUPPORTED;
+        while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
+        stride = sizeof(gcq::gwf::ring);
+        // entries (256-B aligned), records (128 B each), help countdowns (8 B), owners
+        per_tile = ((2 * n * 8 + 255) / 256 * 256) + (size_t)threads_per_tile * (sizeof(gcq::gwf::record) + 8) +
+                   2 * n * 4;
+    } else if (kind == GCQ_GLFQ) {
+        stride = sizeof(gcq::glf::ring);
+        per_tile = 2 * n * 8;
+    } else {
+        const uint64_t max_id = 2ull * ((0xFFFFFFFFull / n) + 1);
+        if (max_id < 2ull * ((uint64_t)threads_per_tile + 1)) return GCQ_EUNSUPPORTED;
+        stride = sizeof(gcq::sfq::queue);
+        per_tile = n * 8;
+    }
+    auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t hdr_bytes = a256(stride * tiles);
+    const size_t tile_bytes = a256(per_tile);
+    char* dq = nullptr;
+    if (cudaMalloc(&dq, hdr_bytes + tile_bytes * tiles + 256) != cudaSuccess) {
+        cudaGetLastError();
+        return GCQ_ENOMEM;
+    }
+    gcq::u32a* d_err = (gcq::u32a*)(dq + hdr_bytes + tile_bytes * tiles);
+    std::vector<char> hh(hdr_bytes, 0);
+    for (int t = 0; t < tiles; ++t) {
+        char* tb = dq + hdr_bytes + tile_bytes * t;
+        if (kind == GCQ_GWFQ) {
+            gcq::gwf::ring r;
+            memset(&r, 0, sizeof r);
+            r.Entry = (gcq::u64a*)tb;
+            r.Record = (gcq::gwf::record*)(tb + a256(2 * n * 8));
+            r.Help = (gcq::gwf::helper_state*)((char*)r.Record + (size_t)threads_per_tile * sizeof(gcq::gwf::record));
+            r.Owner = (gcq::u32a*)((char*)r.Help + (size_t)threads_per_tile * 8);
+            r.err = d_err;
+            r.order = queue_log2;
+            r.thr_bits = (uint32_t)bits;
+            r.max_threads = (uint32_t)threads_per_tile;
+            r.help_delay = WF_HELP_DELAY;
+            r.enq_patience = WF_ENQ_PATIENCE;
+            r.deq_patience = WF_DEQ_PATIENCE;
+            r.remap = 0;
+            r.deq_wait = 0;
+            r.stats = nullptr;
+            memcpy(&hh[t * stride], &r, sizeof r);
+        } else if (kind == GCQ_GLFQ) {
+            gcq::glf::ring r;
+            memset(&r, 0, sizeof r);
+            r.Entry = (gcq::u64a*)tb;
+            r.err = d_err;
+            r.order = queue_log2;
+            r.line_log2 = 3;   // the reference's 64-byte remap (glf_queue.hpp:50-51)
+            r.deq_wait = 0;
+            memcpy(&hh[t * stride], &r, sizeof r);
+        } else {
+            gcq::sfq::queue r;
+            memset(&r, 0, sizeof r);
+            r.slot = (gcq::u64a*)tb;
+            r.err = d_err;
+            r.log2_len = queue_log2;
+            r.max_id = (uint32_t)(2ull * ((0xFFFFFFFFull / n) + 1));
+            r.timeout_ns = timeout_ns;
+            r.nprocs = (uint32_t)threads_per_tile;
+            memcpy(&hh[t * stride], &r, sizeof r);
+        }
+    }
+    cudaError_t e = cudaMemcpy(dq, hh.data(), hdr_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_err, 0, 4);
+    if (e == cudaSuccess) {
+        const dim3 ig((unsigned)std::min<uint64_t>(64, (2 * n + 255) / 256), (unsigned)std::min(tiles, 1024));
+        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(dq, stride, tiles);
+        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(dq, stride, tiles);
+        else k_init_tiles_sfq<<<ig, 256>>>(dq, stride, tiles);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    if (e != cudaSuccess) {
+        cudaFree(dq);
+        return gcqi::cuda_fail(e, "tile rings", __FILE__, __LINE__);
+    }
+    tr->dq = dq;
+    tr->stride = stride;
+    tr->err = d_err;
+    return GCQ_OK;
+}
+
 // ------------------------------------------------ stream-compaction comparator
 // The double-buffer + stream-compaction renderer of concurrent_rt/baselines/
 // rt_compaction.cpp, the non-queue baseline: every pass traces the whole active
@@ -466,107 +891,32 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
     std::vector<Plane> pln;
     build_scene(scene, sph, pln, P);
 
-    // ---- per-tile queues in one allocation
-    size_t stride = 0, per_tile = 0;
-    if (kind == GCQ_GWFQ) {
-        if ((uint64_t)threads_per_tile > n) return GCQ_EUNSUPPORTED;
-        int bits = 5;
-        while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
-        stride = sizeof(gcq::gwf::ring);
-        // entries (256-B aligned), records (128 B each), help countdowns (8 B), owners
-        per_tile = ((2 * n * 8 + 255) / 256 * 256) + (size_t)threads_per_tile * (sizeof(gcq::gwf::record) + 8) +
-                   2 * n * 4;
-        (void)bits;
-    } else if (kind == GCQ_GLFQ) {
-        stride = sizeof(gcq::glf::ring);
-        per_tile = 2 * n * 8;
-    } else {
-        const uint64_t max_id = 2ull * ((0xFFFFFFFFull / n) + 1);
-        if (max_id < 2ull * ((uint64_t)threads_per_tile + 1)) return GCQ_EUNSUPPORTED;
-        stride = sizeof(gcq::sfq::queue);
-        per_tile = n * 8;
-    }
-    auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
-    const size_t hdr_bytes = a256(stride * tiles);
-    const size_t tile_bytes = a256(per_tile);
-    const size_t q_bytes = hdr_bytes + tile_bytes * tiles + 256;
+    tile_rings tr;
+    int rc = make_tile_rings(kind, tiles, threads_per_tile, queue_log2, P.timeout_ns, &tr);
+    if (rc != GCQ_OK) return rc;
+    char* dq = tr.dq;
+    const size_t stride = tr.stride;
+    gcq::u32a* d_err = tr.err;
     const size_t ray_bytes = (size_t)width * height * sizeof(Ray);
     const size_t img_bytes = (size_t)width * height * 3 * sizeof(float);
-    char* dq = nullptr;
     Ray* d_rays = nullptr;
     float* d_img = nullptr;
     unsigned long long* d_cnt = nullptr;   // alive[tiles], traced[tiles]
     Sphere* d_sph = nullptr;
     Plane* d_pln = nullptr;
-    auto cleanup = [&]() { cudaFree(dq); cudaFree(d_rays); cudaFree(d_img); cudaFree(d_cnt); cudaFree(d_sph); cudaFree(d_pln); };
-    if (cudaMalloc(&dq, q_bytes) != cudaSuccess || cudaMalloc(&d_rays, ray_bytes) != cudaSuccess ||
-        cudaMalloc(&d_img, img_bytes) != cudaSuccess || cudaMalloc(&d_cnt, 2 * tiles * 8) != cudaSuccess ||
+    auto cleanup = [&]() { free_tile_rings(&tr); cudaFree(d_rays); cudaFree(d_img); cudaFree(d_cnt); cudaFree(d_sph); cudaFree(d_pln); };
+    if (cudaMalloc(&d_rays, ray_bytes) != cudaSuccess || cudaMalloc(&d_img, img_bytes) != cudaSuccess ||
+        cudaMalloc(&d_cnt, 2 * tiles * 8) != cudaSuccess ||
         cudaMalloc(&d_sph, std::max<size_t>(1, sph.size()) * sizeof(Sphere)) != cudaSuccess ||
         cudaMalloc(&d_pln, std::max<size_t>(1, pln.size()) * sizeof(Plane)) != cudaSuccess) {
+        cudaGetLastError();
         cleanup();
         return GCQ_ENOMEM;
     }
-    gcq::u32a* d_err = (gcq::u32a*)(dq + hdr_bytes + tile_bytes * tiles);
-    {
-        std::vector<char> hh(hdr_bytes, 0);
-        for (int t = 0; t < tiles; ++t) {
-            char* tb = dq + hdr_bytes + tile_bytes * t;
-            if (kind == GCQ_GWFQ) {
-                int bits = 5;
-                while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
-                gcq::gwf::ring r;
-                memset(&r, 0, sizeof r);
-                r.Entry = (gcq::u64a*)tb;
-                r.Record = (gcq::gwf::record*)(tb + a256(2 * n * 8));
-                r.Help = (gcq::gwf::helper_state*)((char*)r.Record + (size_t)threads_per_tile * sizeof(gcq::gwf::record));
-                r.Owner = (gcq::u32a*)((char*)r.Help + (size_t)threads_per_tile * 8);
-                r.err = d_err;
-                r.order = queue_log2;
-                r.thr_bits = (uint32_t)bits;
-                r.max_threads = (uint32_t)threads_per_tile;
-                r.help_delay = WF_HELP_DELAY;
-                r.enq_patience = WF_ENQ_PATIENCE;
-                r.deq_patience = WF_DEQ_PATIENCE;
-                r.remap = 0;
-                r.deq_wait = 0;
-                r.stats = nullptr;
-                memcpy(&hh[t * stride], &r, sizeof r);
-            } else if (kind == GCQ_GLFQ) {
-                gcq::glf::ring r;
-                memset(&r, 0, sizeof r);
-                r.Entry = (gcq::u64a*)tb;
-                r.err = d_err;
-                r.order = queue_log2;
-                r.line_log2 = 3;   // the reference's 64-byte remap (glf_queue.hpp:50-51)
-                r.deq_wait = 0;
-                memcpy(&hh[t * stride], &r, sizeof r);
-            } else {
-                gcq::sfq::queue r;
-                memset(&r, 0, sizeof r);
-                r.slot = (gcq::u64a*)tb;
-                r.err = d_err;
-                r.log2_len = queue_log2;
-                r.max_id = (uint32_t)(2ull * ((0xFFFFFFFFull / n) + 1));
-                r.timeout_ns = P.timeout_ns;
-                r.nprocs = (uint32_t)threads_per_tile;
-                memcpy(&hh[t * stride], &r, sizeof r);
-            }
-        }
-        GCQ_CUDA(cudaMemcpy(dq, hh.data(), hdr_bytes, cudaMemcpyHostToDevice));
-    }
-    GCQ_CUDA(cudaMemset(d_err, 0, 4));
     GCQ_CUDA(cudaMemset(d_img, 0, img_bytes));
     GCQ_CUDA(cudaMemset(d_cnt, 0, 2 * tiles * 8));
     if (!sph.empty()) GCQ_CUDA(cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(Sphere), cudaMemcpyHostToDevice));
     if (!pln.empty()) GCQ_CUDA(cudaMemcpy(d_pln, pln.data(), pln.size() * sizeof(Plane), cudaMemcpyHostToDevice));
-    {
-        const dim3 ig((unsigned)std::min<uint64_t>(64, (2 * n + 255) / 256), (unsigned)std::min(tiles, 1024));
-        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(dq, stride, tiles);
-        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(dq, stride, tiles);
-        else k_init_tiles_sfq<<<ig, 256>>>(dq, stride, tiles);
-        GCQ_CUDA(cudaGetLastError());
-        GCQ_CUDA(cudaDeviceSynchronize());
-    }
     const int TPB = 256;
     const dim3 grid((unsigned)((threads_per_tile + TPB - 1) / TPB), (unsigned)tiles);
     cudaEvent_t e0, e1, e2;
@@ -703,6 +1053,114 @@ int gcq_rt_compact_render(int scene, int width, int height, int max_bounces, flo
     out->leftover = 0;
     cleanup();
     return GCQ_OK;
+}
+
+// Render a benchmark scene with the per-tile ray-bounce queues: tile_px x tile_px
+// tiles, threads_per_tile workers and one queue of 2^queue_log2 per tile, paths of
+// at most max_bounces scattering events from a seed.  kind: GCQ_GWFQ, GCQ_GLFQ or
+// GCQ_SFQ.  image (may be NULL) receives width*height RGB floats.
+int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
+                         int max_bounces, uint32_t queue_log2, uint64_t seed, float* image, gcq_rt_result* out) {
+    if (!out || width <= 0 || height <= 0 || tile_px <= 0 || threads_per_tile <= 0 || max_bounces < 0 ||
+        max_bounces > 1000 || scene < 0 || scene > 1 || queue_log2 < 4 || queue_log2 > 24)
+        return GCQ_EINVAL;
+    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
+    memset(out, 0, sizeof(*out));
+    bparams P;
+    memset(&P, 0, sizeof P);
+    P.img_w = width;
+    P.img_h = height;
+    P.tile_w = P.tile_h = tile_px;
+    P.tiles_x = (width + tile_px - 1) / tile_px;
+    const int tiles_y = (height + tile_px - 1) / tile_px;
+    const int tiles = P.tiles_x * tiles_y;
+    P.threads_per_tile = threads_per_tile;
+    P.max_depth = max_bounces;
+    P.seed = seed;
+    P.timeout_ns = 5000000000ull;
+    if ((uint64_t)tile_px * tile_px > (1ull << queue_log2)) return GCQ_ECAPACITY;   // a tile must fit its queue
+    std::vector<BSphere> sph;
+    std::vector<BQuad> quad;
+    build_bscene(scene, seed, sph, quad, P);
+    tile_rings tr;
+    int rc = make_tile_rings(kind, tiles, threads_per_tile, queue_log2, P.timeout_ns, &tr);
+    if (rc != GCQ_OK) return rc;
+    const size_t npx = (size_t)width * height;
+    BRay* d_rays = nullptr;
+    BPix* d_pix = nullptr;
+    float* d_img = nullptr;
+    unsigned long long* d_cnt = nullptr;
+    BSphere* d_sph = nullptr;
+    BQuad* d_quad = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    auto cleanup = [&]() {
+        free_tile_rings(&tr);
+        cudaFree(d_rays); cudaFree(d_pix); cudaFree(d_img); cudaFree(d_cnt); cudaFree(d_sph); cudaFree(d_quad);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (e2) cudaEventDestroy(e2);
+    };
+    if (cudaMalloc(&d_rays, npx * sizeof(BRay)) != cudaSuccess || cudaMalloc(&d_pix, npx * sizeof(BPix)) != cudaSuccess ||
+        cudaMalloc(&d_img, npx * 12) != cudaSuccess || cudaMalloc(&d_cnt, 2 * (size_t)tiles * 8) != cudaSuccess ||
+        cudaMalloc(&d_sph, std::max<size_t>(1, sph.size()) * sizeof(BSphere)) != cudaSuccess ||
+        cudaMalloc(&d_quad, std::max<size_t>(1, quad.size()) * sizeof(BQuad)) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return GCQ_ENOMEM;
+    }
+    auto fail = [&](cudaError_t e, const char* what) { cleanup(); return gcqi::cuda_fail(e, what, __FILE__, __LINE__); };
+    cudaError_t ce = cudaMemset(d_img, 0, npx * 12);
+    if (ce == cudaSuccess) ce = cudaMemset(d_cnt, 0, 2 * (size_t)tiles * 8);
+    if (ce == cudaSuccess && !sph.empty()) ce = cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(BSphere), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !quad.empty()) ce = cudaMemcpy(d_quad, quad.data(), quad.size() * sizeof(BQuad), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e2);
+    if (ce != cudaSuccess) return fail(ce, "rt bounce setup");
+    const int TPB = 256;
+    const dim3 grid((unsigned)((threads_per_tile + TPB - 1) / TPB), (unsigned)tiles);
+    unsigned long long* d_alive = d_cnt;
+    unsigned long long* d_traced = d_cnt + tiles;
+    const int ns = (int)sph.size(), nq = (int)quad.size();
+    cudaEventRecord(e0);
+    if (kind == GCQ_GWFQ) k_bgen<GCQ_GWFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
+    else if (kind == GCQ_GLFQ) k_bgen<GCQ_GLFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
+    else k_bgen<GCQ_SFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
+    cudaEventRecord(e1);
+    if (kind == GCQ_GWFQ)
+        k_btrace<GCQ_GWFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
+                                          d_traced, tr.err);
+    else if (kind == GCQ_GLFQ)
+        k_btrace<GCQ_GLFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
+                                          d_traced, tr.err);
+    else
+        k_btrace<GCQ_SFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
+                                         d_traced, tr.err);
+    cudaEventRecord(e2);
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e2);
+    if (ce != cudaSuccess) return fail(ce, "rt bounce kernels");
+    float gen_ms = 0, trace_ms = 0;
+    cudaEventElapsedTime(&gen_ms, e0, e1);
+    cudaEventElapsedTime(&trace_ms, e1, e2);
+    std::vector<unsigned long long> cnt(2 * (size_t)tiles);
+    uint32_t err = 0;
+    ce = cudaMemcpy(cnt.data(), d_cnt, 2 * (size_t)tiles * 8, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&err, tr.err, 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && image) ce = cudaMemcpy(image, d_img, npx * 12, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return fail(ce, "rt bounce results");
+    uint64_t leftover = 0, traced = 0;
+    for (int t = 0; t < tiles; ++t) { leftover += cnt[t]; traced += cnt[tiles + t]; }
+    out->gen_ms = gen_ms;
+    out->trace_ms = trace_ms;
+    out->total_ms = gen_ms + trace_ms;
+    out->primary_rays = npx;
+    out->total_rays = traced;
+    out->leftover = leftover;
+    cleanup();
+    if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
+    if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
+    return leftover ? GCQ_EDEVICE : GCQ_OK;
 }
 
 }  // extern "C"

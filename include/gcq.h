@@ -311,6 +311,17 @@ typedef struct gcq_rt_result {
 int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
                   int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out);
 
+/* The ray-tracing workload of the benchmark configuration (no reference
+ * counterpart): scene 0 = 512 seeded spheres (diffuse / metal / glass) over a ground
+ * quad under a sky, scene 1 = a box room with two boxes and a ceiling light; one
+ * sample per pixel, 32-byte rays in per-tile ray-bounce queues (tile_px x tile_px
+ * pixels, threads_per_tile workers, 2^queue_log2 entries per tile), paths of at most
+ * max_bounces scattering events from `seed`.  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ.
+ * Sampling uses integer PCG and rejection, so the image is reproducible bit for bit
+ * on the CPU. */
+int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
+                         int max_bounces, uint32_t queue_log2, uint64_t seed, float* image, gcq_rt_result* out);
+
 /* The stream-compaction baseline (concurrent_rt/baselines/rt_compaction.cpp): the
  * same scenes (plus its scene 2, the mirror tunnel, which gcq_rt_render also
  * accepts), double-buffered ray lists packed in order after every pass, its own

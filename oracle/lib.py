@@ -74,6 +74,8 @@ _EXTRA = [
     ("oracle_bfs", [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p], C.c_int32),
     ("oracle_rt_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p], C.c_int64),
     ("oracle_rt_compact_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p], C.c_int64),
+    ("oracle_rt_bounce_render", [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_void_p],
+     C.c_int64),
     ("oracle_levels_checksum", [C.c_int32, C.c_void_p], C.c_uint64),
     ("oracle_gwf_slow_passed_slot", [C.c_int, C.c_void_p], C.c_int),
 ]

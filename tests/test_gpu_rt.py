@@ -92,3 +92,68 @@ def test_rt_compact_rejects(gcq):
         with pytest.raises(gcq.GcqError) as e:
             gcq.rt_compact_render(**kw)
         assert e.value.status == gcq.EINVAL
+
+
+# ------------------------------------ benchmark scenes: 1024x1024, 1 spp, 4 bounces
+BOUNCE_TOL = 1e-4   # per fp32 channel; the two renders perform the same operations
+
+
+def _bounce_cpu(oracle_lib, scene, w, h, bounces, seed=1):
+    img = np.zeros((h, w, 3), np.float32)
+    n = oracle_lib.lib().oracle_rt_bounce_render(scene, w, h, bounces, seed, 16, img.ctypes.data)
+    assert n > 0
+    return img, n
+
+
+@pytest.fixture(scope="module")
+def bounce_images(oracle_lib):
+    return {s: _bounce_cpu(oracle_lib, s, 1024, 1024, 4) for s in (0, 1)}
+
+
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "sfq"])
+@pytest.mark.parametrize("scene", [0, 1])
+def test_rt_bounce_full_size(gcq, bounce_images, kind, scene):
+    """The benchmark configuration: 1024x1024, 32x32-pixel tiles, 1024 threads per
+    tile, queue 2^15 per tile, 4 bounces; image and ray count equal the serial render."""
+    r, img = gcq.rt_bounce_render(kind, scene=scene)
+    want, rays = bounce_images[scene]
+    assert r["leftover"] == 0
+    assert r["primary_rays"] == 1024 * 1024
+    assert r["total_rays"] == rays
+    diff = np.abs(img - want)
+    assert diff.max() <= BOUNCE_TOL, (float(diff.max()), int((diff > BOUNCE_TOL).sum()))
+    assert np.isfinite(img).all()
+
+
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "sfq"])
+@pytest.mark.parametrize("case", [
+    dict(width=100, height=70, tile_px=32, threads_per_tile=1024, max_bounces=4, queue_log2=10),  # ragged tiles
+    dict(width=96, height=96, tile_px=16, threads_per_tile=40, max_bounces=6, queue_log2=8),      # fewer threads
+    dict(width=64, height=48, tile_px=8, threads_per_tile=512, max_bounces=0, queue_log2=9),      # primary only
+    dict(width=1, height=1, tile_px=32, threads_per_tile=32, max_bounces=4, queue_log2=10),       # one pixel
+])
+@pytest.mark.parametrize("scene", [0, 1])
+def test_rt_bounce_edge_cases(gcq, oracle_lib, kind, case, scene):
+    want, rays = _bounce_cpu(oracle_lib, scene, case["width"], case["height"], case["max_bounces"], seed=7)
+    r, img = gcq.rt_bounce_render(kind, scene=scene, seed=7, **case)
+    assert r["leftover"] == 0 and r["total_rays"] == rays
+    assert np.abs(img - want).max() <= BOUNCE_TOL
+
+
+def test_rt_bounce_seed_changes_scene(gcq, oracle_lib):
+    a = gcq.rt_bounce_render("gwfq", scene=0, width=128, height=128, seed=1)[1]
+    b = gcq.rt_bounce_render("gwfq", scene=0, width=128, height=128, seed=2)[1]
+    want, _ = _bounce_cpu(oracle_lib, 0, 128, 128, 4, seed=2)
+    assert np.abs(a - b).max() > 0.1
+    assert np.abs(b - want).max() <= BOUNCE_TOL
+
+
+def test_rt_bounce_rejects(gcq):
+    for kwargs, status in [(dict(kind="wfq"), gcq.EUNSUPPORTED),
+                           (dict(queue_log2=9), gcq.ECAPACITY),          # a 32x32 tile needs 1024 slots
+                           (dict(scene=2), gcq.EINVAL),
+                           (dict(max_bounces=-1), gcq.EINVAL),
+                           (dict(width=0), gcq.EINVAL)]:
+        with pytest.raises(gcq.GcqError) as e:
+            gcq.rt_bounce_render(**kwargs)
+        assert e.value.status == status, kwargs
