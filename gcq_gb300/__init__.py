@@ -71,7 +71,10 @@ class RtResult(C.Structure):
 class ServeCfg(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("timeout_ns", C.c_uint64), ("max_slots", C.c_uint32),
                 ("threads", C.c_uint32), ("work_log2", C.c_uint32), ("_pad", C.c_uint32),
-                ("run_limit_ns", C.c_uint64), ("work_knobs", Knobs)]
+                ("run_limit_ns", C.c_uint64), ("work_knobs", Knobs),
+                ("rt_scenes", C.c_uint32), ("rt_width", C.c_uint32), ("rt_height", C.c_uint32),
+                ("rt_tile_px", C.c_uint32), ("rt_max_bounces", C.c_uint32), ("rt_slots", C.c_uint32),
+                ("rt_seed", C.c_uint64)]
 
 
 class ServeStats(C.Structure):
@@ -79,7 +82,7 @@ class ServeStats(C.Structure):
                 ("edges", C.c_uint64), ("sweeps", C.c_uint64), ("completed", C.c_uint32),
                 ("error_word", C.c_uint32), ("released", C.c_uint32), ("inflight", C.c_uint32),
                 ("reserved", C.c_uint64), ("work_tail", C.c_uint64 * 2), ("work_head", C.c_uint64 * 2),
-                ("work_threshold", C.c_int32 * 2)]
+                ("work_threshold", C.c_int32 * 2), ("rays", C.c_uint64)]
 
 
 # gcq_serve_req / gcq_serve_res (include/gcq.h)
@@ -138,6 +141,10 @@ SIGNATURES = {
     "gcq_rt_render": ([I32, I32, I32, I32, I32, I32, I32, I32, U32, P, C.POINTER(RtResult)], I32),
     "gcq_rt_compact_render": ([I32, I32, I32, I32, P, C.POINTER(RtResult)], I32),
     "gcq_rt_bounce_render": ([I32, I32, I32, I32, I32, I32, I32, U32, U64, P, C.POINTER(RtResult)], I32),
+    "gcq_rt_ctx_create": ([I32, I32, I32, I32, I32, I32, I32, U32, U64, I32, C.POINTER(P)], I32),
+    "gcq_rt_ctx_render": ([P, P, I32, P, C.POINTER(RtResult)], I32),
+    "gcq_rt_ctx_destroy": ([P], I32),
+    "gcq_serve_image": ([P, I32, P], I32),
     "gcq_tb_autotune": ([I32, U32, U32, I32, I32, C.c_double, U32, C.POINTER(TunePoint), C.POINTER(TunePoint), SZ,
                          C.POINTER(SZ)], I32),
     "gcq_serve_default_cfg": ([C.POINTER(ServeCfg)], None),
@@ -402,19 +409,23 @@ class Bfs:
 
 
 class Server:
-    """Persistent BFS server over resident CSR graphs (gcq_serve_create / gcq_serve_run).
+    """Persistent BFS and ray-tile server over resident CSR graphs and scenes
+    (gcq_serve_create / gcq_serve_run).
 
-    graphs: a list of (offsets, indices) int32 CSR pairs.  run() takes a structured
-    array of SERVE_REQ_DTYPE sorted by arrival_ns and returns (SERVE_RES_DTYPE
-    array, stats dict)."""
+    graphs: a list of (offsets, indices) int32 CSR pairs.  rt_scenes > 0 also serves
+    tiles of the benchmark scenes 0 .. rt_scenes-1 as targets len(graphs) + scene.
+    run() takes a structured array of SERVE_REQ_DTYPE sorted by arrival_ns and
+    returns (SERVE_RES_DTYPE array, stats dict)."""
 
     def __init__(self, graphs, budget_bytes: int | None = None, max_slots: int = 0, threads: int = 0,
-                 work_log2: int = 0, timeout_s: float = 0.0, run_limit_s: float = 0.0, **work_knobs):
+                 work_log2: int = 0, timeout_s: float = 0.0, run_limit_s: float = 0.0, rt_scenes: int = 0,
+                 rt_size=(1024, 1024), rt_tile_px: int = 32, rt_max_bounces: int = 4, rt_slots: int = 0,
+                 rt_seed: int = 1, **work_knobs):
         self.graphs = [(np.ascontiguousarray(o, dtype=np.int32), np.ascontiguousarray(i, dtype=np.int32))
                        for o, i in graphs]
         n = len(self.graphs)
-        offs = (C.c_void_p * n)(*[o.ctypes.data for o, _ in self.graphs])
-        idxs = (C.c_void_p * n)(*[i.ctypes.data for _, i in self.graphs])
+        offs = (C.c_void_p * max(n, 1))(*[o.ctypes.data for o, _ in self.graphs])
+        idxs = (C.c_void_p * max(n, 1))(*[i.ctypes.data for _, i in self.graphs])
         self.V = np.array([len(o) - 1 for o, _ in self.graphs], dtype=np.int32)
         E = np.array([len(i) for _, i in self.graphs], dtype=np.int64)
         cfg = ServeCfg()
@@ -433,6 +444,13 @@ class Server:
             cfg.run_limit_ns = int(run_limit_s * 1e9)
         for name, v in work_knobs.items():   # knobs of the worklist queue
             setattr(cfg.work_knobs, name, v)
+        cfg.rt_scenes = rt_scenes
+        cfg.rt_width, cfg.rt_height = rt_size
+        cfg.rt_tile_px, cfg.rt_max_bounces, cfg.rt_seed = rt_tile_px, rt_max_bounces, rt_seed
+        if rt_slots:
+            cfg.rt_slots = rt_slots
+        self.rt_size = tuple(rt_size)
+        self.rt_tiles = ((rt_size[0] + rt_tile_px - 1) // rt_tile_px) * ((rt_size[1] + rt_tile_px - 1) // rt_tile_px)
         h = P()
         _check(_lib().gcq_serve_create(n, C.cast(offs, P), C.cast(idxs, P), self.V.ctypes.data, E.ctypes.data,
                                        C.byref(cfg), C.byref(h)), "gcq_serve_create")
@@ -454,6 +472,12 @@ class Server:
         self.last_results = res
         _check(rc, "gcq_serve_run")
         return res, self.last_stats
+
+    def image(self, scene: int) -> np.ndarray:
+        """The served scene's image (height x width x 3 float32)."""
+        img = np.zeros((self.rt_size[1], self.rt_size[0], 3), dtype=np.float32)
+        _check(_lib().gcq_serve_image(self._h, scene, img.ctypes.data), "gcq_serve_image")
+        return img
 
     def close(self):
         if self._h:
@@ -486,6 +510,29 @@ def serve_requests(n: int, ngraphs: int, V, rate_per_s: float = 0.0, seed: int =
     return r
 
 
+def tile_checksum(img: np.ndarray, tile: int, tile_px: int = 32) -> int:
+    """The checksum a served tile reports (gcq_serve_res.checksum), from an image."""
+    h, w = img.shape[:2]
+    tx = (w + tile_px - 1) // tile_px
+    x0, y0 = (tile % tx) * tile_px, (tile // tx) * tile_px
+    ys, xs = np.mgrid[y0:min(y0 + tile_px, h), x0:min(x0 + tile_px, w)]
+    g = (ys * w + xs).reshape(-1).astype(np.uint64)
+    bits = img[y0:y0 + tile_px, x0:x0 + tile_px].reshape(-1, 3).view(np.uint32).astype(np.uint64)
+    key = ((3 * g[:, None] + np.arange(3, dtype=np.uint64)[None, :]) << np.uint64(32)) | bits
+    with np.errstate(over="ignore"):
+        return int(splitmix64(key.reshape(-1)).sum(dtype=np.uint64))
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    """splitmix64 finaliser over a uint64 array (as the library's checksums use it)."""
+    x = np.asarray(x, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
 def rt_render(kind: str = "gwfq", scene: int = 0, width: int = 1280, height: int = 720, tiles_x: int = 8,
               tiles_y: int = 8, threads_per_tile: int = 1024, max_bounces: int = 4, queue_log2: int = 15):
     """Render one frame with the persistent per-tile ray tracer; returns (result, image HxWx3)."""
@@ -504,6 +551,42 @@ def rt_bounce_render(kind: str = "gwfq", scene: int = 0, width: int = 1024, heig
     _check(_lib().gcq_rt_bounce_render(KINDS[kind], scene, width, height, tile_px, threads_per_tile, max_bounces,
                                        queue_log2, seed, img.ctypes.data, C.byref(r)), "gcq_rt_bounce_render")
     return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
+
+
+class RtTiles:
+    """A benchmark-scene render context (gcq_rt_ctx_*): renders lists of tiles."""
+
+    def __init__(self, kind: str = "gwfq", scene: int = 0, width: int = 1024, height: int = 1024, tile_px: int = 32,
+                 threads_per_tile: int = 1024, max_bounces: int = 4, queue_log2: int = 15, seed: int = 1,
+                 max_tiles: int = 0):
+        self.width, self.height = width, height
+        self._h = P()
+        _check(_lib().gcq_rt_ctx_create(KINDS[kind], scene, width, height, tile_px, threads_per_tile, max_bounces,
+                                        queue_log2, seed, max_tiles, C.byref(self._h)), "gcq_rt_ctx_create")
+
+    def render(self, tiles=None, image: bool = False):
+        """Render the tiles (sequence of tile indices, None: all); returns (result, image or None)."""
+        img = np.zeros((self.height, self.width, 3), dtype=np.float32) if image else None
+        r = RtResult()
+        if tiles is None:
+            lst, n, ptr = None, 0, None
+        else:
+            lst = np.ascontiguousarray(tiles, dtype=np.int32)
+            n, ptr = len(lst), lst.ctypes.data
+        _check(_lib().gcq_rt_ctx_render(self._h, ptr, n, img.ctypes.data if image else None, C.byref(r)),
+               "gcq_rt_ctx_render")
+        return {f: getattr(r, f) for f, _ in RtResult._fields_}, img
+
+    def close(self):
+        if self._h:
+            _lib().gcq_rt_ctx_destroy(self._h)
+            self._h = P()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def rt_compact_render(scene: int = 0, width: int = 1280, height: int = 720, max_bounces: int = 4):

@@ -33,7 +33,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "-I" + INCLUDE, "-I" + CSRC]
 # Per-file extra flags: the ray tracer's device float math must round exactly like
 # the CPU reference render, so it is compiled without FMA contraction.
-EXTRA = {"gcq_rt.cu": ["--fmad=false"]}
+EXTRA = {"gcq_rt.cu": ["--fmad=false"], "gcq_serve.cu": ["--fmad=false"]}
 
 
 def nvcc() -> str:

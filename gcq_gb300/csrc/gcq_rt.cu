@@ -13,25 +13,9 @@
 #include <cstring>
 #include <vector>
 
-#include "gcq_internal.cuh"
+#include "gcq_scene.cuh"
 
 namespace {
-
-struct V3 { float x, y, z; };
-__host__ __device__ __forceinline__ V3 v3(float x, float y, float z) { V3 r; r.x = x; r.y = y; r.z = z; return r; }
-__host__ __device__ __forceinline__ V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__host__ __device__ __forceinline__ V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__host__ __device__ __forceinline__ V3 scale(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
-__host__ __device__ __forceinline__ V3 mulv(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
-__host__ __device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__host__ __device__ __forceinline__ V3 normalize(V3 v) {
-    const float d = sqrtf(dot3(v, v));
-    return d > 0.f ? scale(v, 1.f / d) : v;
-}
-__host__ __device__ __forceinline__ V3 reflect3(V3 v, V3 n) { return sub(v, scale(n, 2.f * dot3(v, n))); }
-__host__ __device__ __forceinline__ V3 clamp01(V3 c) {
-    return v3(fminf(fmaxf(c.x, 0.f), 1.f), fminf(fmaxf(c.y, 0.f), 1.f), fminf(fmaxf(c.z, 0.f), 1.f));
-}
 
 // rt_final.cpp:350-366
 struct Sphere { V3 c; float r; V3 albedo; float refl; };
@@ -313,217 +297,53 @@ void build_scene(int scene, std::vector<Sphere>& sph, std::vector<Plane>& pln, r
 
 
 
-// ------------------------------------------------ benchmark scenes, 1 sample/pixel
-// The ray-tracing workload of the benchmark configuration (the reference has no
-// such scenes; its two scenes are above): 1024x1024 pixels in 32x32-pixel tiles,
-// one sample per pixel, 32-byte rays (origin, direction, pixel id, depth) in the
-// per-tile ray-bounce queues.  Scene 0: 512 seeded spheres (60 % diffuse, 30 % metal,
-// 10 % glass) over a 40 x 40 ground quad under a sky.  Scene 1: a box room of five
-// diffuse quads, two axis-aligned boxes and an emitting ceiling quad.  A path
-// scatters per material (Lambertian, fuzzy metal, glass with Schlick reflectance)
-// until it leaves the scene, reaches the light, is absorbed or uses up max_bounces;
-// a pixel's one path contributes once, so the image needs no float atomics.
-// Sampling uses no transcendental function (PCG integers, rejection sampling,
-// Schlick as products), so the render is bit-identical to its CPU restatement.
-struct BRay { V3 o, d; uint32_t pix, depth; };   // 32 bytes
-struct BPix { V3 tp; uint32_t rng; };            // path throughput and RNG state, per pixel
-enum { B_DIFFUSE = 0, B_METAL = 1, B_GLASS = 2, B_LIGHT = 3 };
-struct BSphere { V3 c; float r; V3 albedo; float param; int mat; int _p[3]; };   // param: fuzz or index
-struct BQuad { int axis; float k, a0, a1, b0, b1; V3 albedo; int mat; };          // axis-aligned rectangle
-struct BCam { V3 o, lower_left, horiz, vert; };
-struct BHit { float t; V3 p, n; V3 albedo; float param; int mat; bool front, did_hit; };
-struct bparams {
-    int img_w, img_h, tiles_x, tile_w, tile_h, threads_per_tile, max_depth, sky;
-    BCam cam;
-    uint64_t seed, timeout_ns;
-};
-
-__host__ __device__ __forceinline__ float comp(V3 v, int i) { return i == 0 ? v.x : i == 1 ? v.y : v.z; }
-__host__ __device__ __forceinline__ uint32_t pcg_next(uint32_t& s) {
-    s = s * 747796405u + 2891336453u;
-    const uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
-    return (w >> 22u) ^ w;
-}
-__host__ __device__ __forceinline__ float rand01(uint32_t& s) { return (float)(pcg_next(s) >> 8) * (1.0f / 16777216.0f); }
-__device__ __forceinline__ V3 rand_in_unit_sphere(uint32_t& s) {
-    for (int k = 0; k < 64; ++k) {
-        const float x = 2.f * rand01(s) - 1.f;
-        const float y = 2.f * rand01(s) - 1.f;
-        const float z = 2.f * rand01(s) - 1.f;
-        const V3 p = v3(x, y, z);
-        if (dot3(p, p) < 1.f) return p;
-    }
-    return v3(0.f, 0.f, 0.f);
-}
-
-__device__ __forceinline__ bool bhit_sphere(const BRay& r, const BSphere& sp, float tmax, BHit& h) {
-    const V3 oc = sub(r.o, sp.c);
-    const float a = dot3(r.d, r.d);
-    const float half_b = dot3(oc, r.d);
-    const float c = dot3(oc, oc) - sp.r * sp.r;
-    const float disc = half_b * half_b - a * c;
-    if (disc < 0.f) return false;
-    const float sq = sqrtf(disc);
-    float root = (-half_b - sq) / a;
-    if (root <= 1e-3f || root >= tmax) {
-        root = (-half_b + sq) / a;
-        if (root <= 1e-3f || root >= tmax) return false;
-    }
-    h.t = root;
-    h.p = add(r.o, scale(r.d, root));
-    const V3 outward = scale(sub(h.p, sp.c), 1.f / sp.r);
-    h.front = dot3(r.d, outward) < 0.f;
-    h.n = h.front ? outward : scale(outward, -1.f);
-    h.albedo = sp.albedo;
-    h.param = sp.param;
-    h.mat = sp.mat;
-    h.did_hit = true;
-    return true;
-}
-__device__ __forceinline__ bool bhit_quad(const BRay& r, const BQuad& q, float tmax, BHit& h) {
-    const float da = comp(r.d, q.axis);
-    if (fabsf(da) < 1e-8f) return false;
-    const float t = (q.k - comp(r.o, q.axis)) / da;
-    if (t <= 1e-3f || t >= tmax) return false;
-    const V3 p = add(r.o, scale(r.d, t));
-    const float u = q.axis == 0 ? p.y : p.x;
-    const float w = q.axis == 2 ? p.y : p.z;
-    if (u < q.a0 || u > q.a1 || w < q.b0 || w > q.b1) return false;
-    h.t = t;
-    h.p = p;
-    const V3 outward = v3(q.axis == 0 ? 1.f : 0.f, q.axis == 1 ? 1.f : 0.f, q.axis == 2 ? 1.f : 0.f);
-    h.front = da < 0.f;
-    h.n = h.front ? outward : scale(outward, -1.f);
-    h.albedo = q.albedo;
-    h.param = 0.f;
-    h.mat = q.mat;
-    h.did_hit = true;
-    return true;
-}
-__device__ __forceinline__ BHit btrace(const BRay& r, const BSphere* sph, int ns, const BQuad* quad, int nq) {
-    BHit best;
-    best.did_hit = false;
-    best.t = 1e30f;
-    for (int i = 0; i < ns; ++i) {
-        BHit h;
-        if (bhit_sphere(r, sph[i], best.t, h)) best = h;
-    }
-    for (int i = 0; i < nq; ++i) {
-        BHit h;
-        if (bhit_quad(r, quad[i], best.t, h)) best = h;
-    }
-    return best;
-}
-
-// One bounce of a path: true with r and st updated when the path continues; false
-// with *contrib set when it ends.
-__device__ __forceinline__ bool bshade(BRay& r, BPix& st, const BHit& hit, const bparams& P, V3* contrib) {
-    if (!hit.did_hit) {
-        if (P.sky) {
-            const V3 unit = normalize(r.d);
-            const float t = 0.5f * (unit.y + 1.f);
-            const V3 sky = add(scale(v3(1.f, 1.f, 1.f), 1.f - t), scale(v3(0.5f, 0.7f, 1.f), t));
-            *contrib = mulv(st.tp, sky);
-        } else {
-            *contrib = v3(0.f, 0.f, 0.f);
-        }
-        return false;
-    }
-    if (hit.mat == B_LIGHT) {
-        *contrib = mulv(st.tp, hit.albedo);
-        return false;
-    }
-    if ((int)r.depth >= P.max_depth) {
-        *contrib = v3(0.f, 0.f, 0.f);
-        return false;
-    }
-    V3 dir;
-    V3 att = hit.albedo;
-    if (hit.mat == B_DIFFUSE) {
-        dir = add(hit.n, normalize(rand_in_unit_sphere(st.rng)));
-        if (fabsf(dir.x) < 1e-8f && fabsf(dir.y) < 1e-8f && fabsf(dir.z) < 1e-8f) dir = hit.n;
-    } else if (hit.mat == B_METAL) {
-        const V3 refl = reflect3(normalize(r.d), hit.n);
-        dir = add(refl, scale(rand_in_unit_sphere(st.rng), hit.param));
-        if (dot3(dir, hit.n) <= 0.f) {
-            *contrib = v3(0.f, 0.f, 0.f);
-            return false;
-        }
-    } else {
-        const float ratio = hit.front ? 1.f / hit.param : hit.param;
-        const V3 unit = normalize(r.d);
-        const float cos_t = fminf(dot3(scale(unit, -1.f), hit.n), 1.f);
-        const float sin_t = sqrtf(1.f - cos_t * cos_t);
-        float r0 = (1.f - ratio) / (1.f + ratio);
-        r0 = r0 * r0;
-        const float x = 1.f - cos_t;
-        const float schlick = r0 + (1.f - r0) * (x * x * x * x * x);
-        const float u = rand01(st.rng);
-        if (ratio * sin_t > 1.f || schlick > u) {
-            dir = reflect3(unit, hit.n);
-        } else {
-            const V3 perp = scale(add(unit, scale(hit.n, cos_t)), ratio);
-            const V3 par = scale(hit.n, -sqrtf(fabsf(1.f - dot3(perp, perp))));
-            dir = add(perp, par);
-        }
-        att = v3(1.f, 1.f, 1.f);
-    }
-    r.o = hit.p;
-    r.d = normalize(dir);
-    r.depth += 1;
-    st.tp = mulv(st.tp, att);
-    return true;
-}
+// Path tracing of the benchmark scenes (scene code in gcq_scene.cuh) over the
+// per-tile queues.  blockIdx.y = j, the position in a list of tiles (tile = list[j],
+// or j without a list); ring j serves it and its rays and path states live at
+// [j * tile pixels, +tile pixels).
+__device__ __forceinline__ int btile(const int32_t* list, int j) { return list ? list[j] : j; }
 
 // primary rays of a tile into its queue (as k_generate)
 template <int K>
-__global__ void k_bgen(char* rings, size_t stride, BRay* __restrict__ rays, BPix* __restrict__ pix, bparams P,
-                       unsigned long long* __restrict__ alive) {
-    const int tile = (int)blockIdx.y;
+__global__ void k_bgen(char* rings, size_t stride, const int32_t* __restrict__ list, BRay* __restrict__ rays,
+                       BPix* __restrict__ pix, bparams P, unsigned long long* __restrict__ alive) {
+    const int j = (int)blockIdx.y;
     const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (tid >= P.threads_per_tile) return;
-    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
-    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)j * stride);
+    const int tile = btile(list, j);
+    const int x0 = (tile % P.tiles_x) * P.tile_w, y0 = (tile / P.tiles_x) * P.tile_h;
     const int tw = min(P.tile_w, P.img_w - x0), th = min(P.tile_h, P.img_h - y0);
+    const size_t base = (size_t)j * P.tile_w * P.tile_h;
     int enqueued = 0;
     for (int i = tid; i < tw * th; i += P.threads_per_tile) {
         const int px = x0 + i % tw, py = y0 + i / tw;
-        const uint32_t g = (uint32_t)(py * P.img_w + px);
-        const float s = ((float)px + 0.5f) / (float)P.img_w;
-        const float t = 1.0f - ((float)py + 0.5f) / (float)P.img_h;
         BRay r;
-        r.o = P.cam.o;
-        r.d = normalize(sub(add(add(P.cam.lower_left, scale(P.cam.horiz, s)), scale(P.cam.vert, t)), P.cam.o));
-        r.pix = g;
-        r.depth = 0;
         BPix st;
-        st.tp = v3(1.f, 1.f, 1.f);
-        st.rng = (uint32_t)gcqi::splitmix64(P.seed ^ ((uint64_t)g << 20)) | 1u;
-        rays[g] = r;
-        pix[g] = st;
+        bprimary(P, px, py, (uint32_t)(py * P.img_w + px), &r, &st);
+        rays[base + i] = r;
+        pix[base + i] = st;
         if (rtq<K>::enq(q, (uint32_t)i, (uint32_t)tid)) ++enqueued;   // release publishes the ray
     }
-    if (enqueued > 0) atomicAdd(&alive[tile], (unsigned long long)enqueued);
+    if (enqueued > 0) atomicAdd(&alive[j], (unsigned long long)enqueued);
 }
 
 template <int K>
-__global__ void k_btrace(char* rings, size_t stride, const BSphere* __restrict__ sph, int ns,
-                         const BQuad* __restrict__ quad, int nq, BRay* __restrict__ rays, BPix* __restrict__ pix,
-                         float* __restrict__ img, bparams P, unsigned long long* __restrict__ alive,
-                         unsigned long long* __restrict__ traced, gcq::u32a* err) {
-    const int tile = (int)blockIdx.y;
+__global__ void k_btrace(char* rings, size_t stride, const int32_t* __restrict__ list,
+                         const BSphere* __restrict__ sph, int ns, const BQuad* __restrict__ quad, int nq,
+                         BRay* __restrict__ rays, BPix* __restrict__ pix, float* __restrict__ img, bparams P,
+                         unsigned long long* __restrict__ alive, unsigned long long* __restrict__ traced,
+                         gcq::u32a* err) {
+    const int j = (int)blockIdx.y;
     const int tid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (tid >= P.threads_per_tile) return;
-    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)tile * stride);
-    const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-    const int x0 = tx * P.tile_w, y0 = ty * P.tile_h;
-    const int tw = min(P.tile_w, P.img_w - x0);
+    auto* q = reinterpret_cast<typename rtq<K>::R*>(rings + (size_t)j * stride);
+    const size_t base = (size_t)j * P.tile_w * P.tile_h;
     unsigned long long local_traced = 0;
     gcq::backoff bo;
     uint64_t last_progress = gcq::globaltimer_ns();
     for (uint32_t it = 0;; ++it) {
-        if (gcq::ld_rlx((const gcq::u64a*)&alive[tile]) == 0) break;
+        if (gcq::ld_rlx((const gcq::u64a*)&alive[j]) == 0) break;
         uint32_t li;
         if (!rtq<K>::deq(q, &li, (uint32_t)tid)) {
             if ((it & 63) == 0 && gcq::globaltimer_ns() - last_progress > P.timeout_ns) {
@@ -535,98 +355,22 @@ __global__ void k_btrace(char* rings, size_t stride, const BSphere* __restrict__
         }
         bo = gcq::backoff();
         last_progress = gcq::globaltimer_ns();
-        const uint32_t g = (uint32_t)((y0 + (int)li / tw) * P.img_w + (x0 + (int)li % tw));
-        BRay r = rays[g];
-        BPix st = pix[g];
+        BRay r = rays[base + li];
+        BPix st = pix[base + li];
         const BHit hit = btrace(r, sph, ns, quad, nq);
         ++local_traced;
         V3 c;
         if (bshade(r, st, hit, P, &c)) {
-            rays[g] = r;
-            pix[g] = st;
-            if (!rtq<K>::enq(q, li, (uint32_t)tid)) atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+            rays[base + li] = r;
+            pix[base + li] = st;
+            if (!rtq<K>::enq(q, li, (uint32_t)tid)) atomicAdd(&alive[j], (unsigned long long)(-1LL));
         } else {
-            float* o = img + 3 * (size_t)g;
+            float* o = img + 3 * (size_t)r.pix;
             o[0] = c.x; o[1] = c.y; o[2] = c.z;
-            atomicAdd(&alive[tile], (unsigned long long)(-1LL));
+            atomicAdd(&alive[j], (unsigned long long)(-1LL));
         }
     }
-    if (local_traced > 0) atomicAdd(&traced[tile], local_traced);
-}
-
-uint64_t bscene_rand(uint64_t& s) {
-    s += 0x9e3779b97f4a7c15ULL;
-    return gcqi::splitmix64(s - 0x9e3779b97f4a7c15ULL);
-}
-float bscene_u01(uint64_t& s) { return (float)(bscene_rand(s) >> 40) * (1.0f / 16777216.0f); }
-
-BCam make_bcam(V3 from, V3 at, float half_h, float aspect) {
-    const V3 w = normalize(sub(from, at));
-    const V3 vup = v3(0.f, 1.f, 0.f);
-    const V3 u = normalize(v3(vup.y * w.z - vup.z * w.y, vup.z * w.x - vup.x * w.z, vup.x * w.y - vup.y * w.x));
-    const V3 v = v3(w.y * u.z - w.z * u.y, w.z * u.x - w.x * u.z, w.x * u.y - w.y * u.x);
-    BCam c;
-    c.o = from;
-    c.horiz = scale(u, 2.f * half_h * aspect);
-    c.vert = scale(v, 2.f * half_h);
-    c.lower_left = sub(sub(sub(from, scale(c.horiz, 0.5f)), scale(c.vert, 0.5f)), w);
-    return c;
-}
-
-void add_box(std::vector<BQuad>& q, V3 lo, V3 hi, V3 albedo) {
-    q.push_back({0, lo.x, lo.y, hi.y, lo.z, hi.z, albedo, B_DIFFUSE});
-    q.push_back({0, hi.x, lo.y, hi.y, lo.z, hi.z, albedo, B_DIFFUSE});
-    q.push_back({1, lo.y, lo.x, hi.x, lo.z, hi.z, albedo, B_DIFFUSE});
-    q.push_back({1, hi.y, lo.x, hi.x, lo.z, hi.z, albedo, B_DIFFUSE});
-    q.push_back({2, lo.z, lo.x, hi.x, lo.y, hi.y, albedo, B_DIFFUSE});
-    q.push_back({2, hi.z, lo.x, hi.x, lo.y, hi.y, albedo, B_DIFFUSE});
-}
-
-void build_bscene(int scene, uint64_t seed, std::vector<BSphere>& sph, std::vector<BQuad>& quad, bparams& P) {
-    const float aspect = (float)P.img_w / (float)P.img_h;
-    if (scene == 0) {
-        quad.push_back({1, 0.f, -20.f, 20.f, -20.f, 20.f, v3(0.5f, 0.5f, 0.5f), B_DIFFUSE});
-        uint64_t s = seed;
-        for (int i = 0; i < 512; ++i) {
-            const float r = 0.2f + 0.8f * bscene_u01(s);
-            const float x = -20.f + 40.f * bscene_u01(s);
-            const float z = -20.f + 40.f * bscene_u01(s);
-            const float m = bscene_u01(s);
-            BSphere b;
-            memset(&b, 0, sizeof b);
-            b.c = v3(x, r, z);
-            b.r = r;
-            if (m < 0.6f) {
-                const float a0 = bscene_u01(s), a1 = bscene_u01(s), a2 = bscene_u01(s);
-                b.albedo = v3(a0 * a0, a1 * a1, a2 * a2);
-                b.mat = B_DIFFUSE;
-            } else if (m < 0.9f) {
-                const float a0 = bscene_u01(s), a1 = bscene_u01(s), a2 = bscene_u01(s), f = bscene_u01(s);
-                b.albedo = v3(0.5f + 0.5f * a0, 0.5f + 0.5f * a1, 0.5f + 0.5f * a2);
-                b.param = 0.5f * f;
-                b.mat = B_METAL;
-            } else {
-                b.albedo = v3(1.f, 1.f, 1.f);
-                b.param = 1.5f;
-                b.mat = B_GLASS;
-            }
-            sph.push_back(b);
-        }
-        P.sky = 1;
-        P.cam = make_bcam(v3(13.f, 2.f, 3.f), v3(0.f, 0.f, 0.f), 0.17632698f /* tan 10 deg */, aspect);
-    } else {
-        const V3 white = v3(0.73f, 0.73f, 0.73f);
-        quad.push_back({1, 0.f, -1.f, 1.f, -1.f, 1.f, white, B_DIFFUSE});                           // floor
-        quad.push_back({1, 2.f, -1.f, 1.f, -1.f, 1.f, white, B_DIFFUSE});                           // ceiling
-        quad.push_back({2, -1.f, -1.f, 1.f, 0.f, 2.f, white, B_DIFFUSE});                           // back
-        quad.push_back({0, -1.f, 0.f, 2.f, -1.f, 1.f, v3(0.65f, 0.05f, 0.05f), B_DIFFUSE});         // left
-        quad.push_back({0, 1.f, 0.f, 2.f, -1.f, 1.f, v3(0.12f, 0.45f, 0.15f), B_DIFFUSE});          // right
-        quad.push_back({1, 1.999f, -0.3f, 0.3f, -0.3f, 0.3f, v3(15.f, 15.f, 15.f), B_LIGHT});      // light
-        add_box(quad, v3(-0.6f, 0.f, -0.6f), v3(-0.1f, 1.2f, -0.1f), white);
-        add_box(quad, v3(0.15f, 0.f, 0.f), v3(0.65f, 0.6f, 0.5f), white);
-        P.sky = 0;
-        P.cam = make_bcam(v3(0.f, 1.f, 3.4f), v3(0.f, 1.f, 0.f), 0.36397023f /* tan 20 deg */, aspect);
-    }
+    if (local_traced > 0) atomicAdd(&traced[j], local_traced);
 }
 
 // ---------------------------------------------------------------- per-tile rings
@@ -862,6 +606,28 @@ __global__ void __launch_bounds__(256) k_cscatter(const CRay* __restrict__ tmp, 
 
 }  // namespace
 
+struct gcq_rt_ctx {
+    int kind = 0, tiles = 0, max_tiles = 0, ns = 0, nq = 0;
+    bool fresh = false;      // rings initialised and unused
+    bparams P;
+    tile_rings tr;
+    BRay* rays = nullptr;
+    BPix* pix = nullptr;
+    float* img = nullptr;
+    unsigned long long* cnt = nullptr;   // alive[max_tiles], traced[max_tiles]
+    int32_t* list = nullptr;
+    BSphere* sph = nullptr;
+    BQuad* quad = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    ~gcq_rt_ctx() {
+        free_tile_rings(&tr);
+        cudaFree(rays); cudaFree(pix); cudaFree(img); cudaFree(cnt); cudaFree(list); cudaFree(sph); cudaFree(quad);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (e2) cudaEventDestroy(e2);
+    }
+};
+
 extern "C" {
 
 // Render one frame (rt_final.cpp:705-1018).  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ
@@ -1055,112 +821,160 @@ int gcq_rt_compact_render(int scene, int width, int height, int max_bounces, flo
     return GCQ_OK;
 }
 
-// Render a benchmark scene with the per-tile ray-bounce queues: tile_px x tile_px
-// tiles, threads_per_tile workers and one queue of 2^queue_log2 per tile, paths of
-// at most max_bounces scattering events from a seed.  kind: GCQ_GWFQ, GCQ_GLFQ or
-// GCQ_SFQ.  image (may be NULL) receives width*height RGB floats.
-int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
-                         int max_bounces, uint32_t queue_log2, uint64_t seed, float* image, gcq_rt_result* out) {
-    if (!out || width <= 0 || height <= 0 || tile_px <= 0 || threads_per_tile <= 0 || max_bounces < 0 ||
-        max_bounces > 1000 || scene < 0 || scene > 1 || queue_log2 < 4 || queue_log2 > 24)
+// A render context for the benchmark scenes: scene, rings for up to max_tiles tiles
+// at a time, ray and path storage for them and the image, all allocated once.
+int gcq_rt_ctx_create(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
+                      int max_bounces, uint32_t queue_log2, uint64_t seed, int max_tiles, gcq_rt_ctx** out) {
+    if (!out) return GCQ_EINVAL;
+    *out = nullptr;
+    if (width <= 0 || height <= 0 || tile_px <= 0 || threads_per_tile <= 0 || max_bounces < 0 ||
+        max_bounces > 1000 || scene < 0 || scene > 1 || queue_log2 < 4 || queue_log2 > 24 ||
+        (int64_t)width * height > (1ll << 30))
         return GCQ_EINVAL;
     if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
-    memset(out, 0, sizeof(*out));
-    bparams P;
+    if ((uint64_t)tile_px * tile_px > (1ull << queue_log2)) return GCQ_ECAPACITY;   // a tile must fit its queue
+    gcq_rt_ctx* c = new gcq_rt_ctx();
+    bparams& P = c->P;
     memset(&P, 0, sizeof P);
     P.img_w = width;
     P.img_h = height;
     P.tile_w = P.tile_h = tile_px;
     P.tiles_x = (width + tile_px - 1) / tile_px;
-    const int tiles_y = (height + tile_px - 1) / tile_px;
-    const int tiles = P.tiles_x * tiles_y;
+    c->tiles = P.tiles_x * ((height + tile_px - 1) / tile_px);
+    c->max_tiles = (max_tiles <= 0 || max_tiles > c->tiles) ? c->tiles : max_tiles;
     P.threads_per_tile = threads_per_tile;
     P.max_depth = max_bounces;
     P.seed = seed;
     P.timeout_ns = 5000000000ull;
-    if ((uint64_t)tile_px * tile_px > (1ull << queue_log2)) return GCQ_ECAPACITY;   // a tile must fit its queue
+    c->kind = kind;
     std::vector<BSphere> sph;
     std::vector<BQuad> quad;
     build_bscene(scene, seed, sph, quad, P);
-    tile_rings tr;
-    int rc = make_tile_rings(kind, tiles, threads_per_tile, queue_log2, P.timeout_ns, &tr);
-    if (rc != GCQ_OK) return rc;
-    const size_t npx = (size_t)width * height;
-    BRay* d_rays = nullptr;
-    BPix* d_pix = nullptr;
-    float* d_img = nullptr;
-    unsigned long long* d_cnt = nullptr;
-    BSphere* d_sph = nullptr;
-    BQuad* d_quad = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
-    auto cleanup = [&]() {
-        free_tile_rings(&tr);
-        cudaFree(d_rays); cudaFree(d_pix); cudaFree(d_img); cudaFree(d_cnt); cudaFree(d_sph); cudaFree(d_quad);
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-        if (e2) cudaEventDestroy(e2);
-    };
-    if (cudaMalloc(&d_rays, npx * sizeof(BRay)) != cudaSuccess || cudaMalloc(&d_pix, npx * sizeof(BPix)) != cudaSuccess ||
-        cudaMalloc(&d_img, npx * 12) != cudaSuccess || cudaMalloc(&d_cnt, 2 * (size_t)tiles * 8) != cudaSuccess ||
-        cudaMalloc(&d_sph, std::max<size_t>(1, sph.size()) * sizeof(BSphere)) != cudaSuccess ||
-        cudaMalloc(&d_quad, std::max<size_t>(1, quad.size()) * sizeof(BQuad)) != cudaSuccess) {
+    c->ns = (int)sph.size();
+    c->nq = (int)quad.size();
+    int rc = make_tile_rings(kind, c->max_tiles, threads_per_tile, queue_log2, P.timeout_ns, &c->tr);
+    if (rc != GCQ_OK) { delete c; return rc; }
+    const size_t npx = (size_t)width * height, tpx = (size_t)tile_px * tile_px * c->max_tiles;
+    if (cudaMalloc(&c->rays, tpx * sizeof(BRay)) != cudaSuccess || cudaMalloc(&c->pix, tpx * sizeof(BPix)) != cudaSuccess ||
+        cudaMalloc(&c->img, npx * 12) != cudaSuccess || cudaMalloc(&c->cnt, 2 * (size_t)c->max_tiles * 8) != cudaSuccess ||
+        cudaMalloc(&c->list, (size_t)c->max_tiles * 4) != cudaSuccess ||
+        cudaMalloc(&c->sph, std::max<size_t>(1, sph.size()) * sizeof(BSphere)) != cudaSuccess ||
+        cudaMalloc(&c->quad, std::max<size_t>(1, quad.size()) * sizeof(BQuad)) != cudaSuccess) {
         cudaGetLastError();
-        cleanup();
+        delete c;
         return GCQ_ENOMEM;
     }
-    auto fail = [&](cudaError_t e, const char* what) { cleanup(); return gcqi::cuda_fail(e, what, __FILE__, __LINE__); };
-    cudaError_t ce = cudaMemset(d_img, 0, npx * 12);
-    if (ce == cudaSuccess) ce = cudaMemset(d_cnt, 0, 2 * (size_t)tiles * 8);
-    if (ce == cudaSuccess && !sph.empty()) ce = cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(BSphere), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess && !quad.empty()) ce = cudaMemcpy(d_quad, quad.data(), quad.size() * sizeof(BQuad), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
-    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
-    if (ce == cudaSuccess) ce = cudaEventCreate(&e2);
-    if (ce != cudaSuccess) return fail(ce, "rt bounce setup");
+    cudaError_t ce = cudaMemset(c->img, 0, npx * 12);
+    if (ce == cudaSuccess && !sph.empty()) ce = cudaMemcpy(c->sph, sph.data(), sph.size() * sizeof(BSphere), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !quad.empty()) ce = cudaMemcpy(c->quad, quad.data(), quad.size() * sizeof(BQuad), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&c->e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&c->e1);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&c->e2);
+    if (ce != cudaSuccess) {
+        delete c;
+        return gcqi::cuda_fail(ce, "rt context", __FILE__, __LINE__);
+    }
+    c->fresh = true;
+    *out = c;
+    return GCQ_OK;
+}
+
+int gcq_rt_ctx_destroy(gcq_rt_ctx* c) {
+    if (!c) return GCQ_EINVAL;
+    delete c;
+    return GCQ_OK;
+}
+
+// Render the listed tiles (row-major tile indices; NULL: every tile, in order)
+// into the context's image; image (may be NULL) receives the whole image.
+int gcq_rt_ctx_render(gcq_rt_ctx* c, const int32_t* tiles, int ntiles, float* image, gcq_rt_result* out) {
+    if (!c || !out || (tiles && (ntiles <= 0 || ntiles > c->max_tiles))) return GCQ_EINVAL;
+    if (!tiles) {
+        if (c->max_tiles < c->tiles) return GCQ_EINVAL;
+        ntiles = c->tiles;
+    }
+    const bparams& P = c->P;
+    uint64_t primary = 0;
+    if (tiles) {
+        for (int j = 0; j < ntiles; ++j) {
+            if (tiles[j] < 0 || tiles[j] >= c->tiles) return GCQ_EINVAL;
+            const int x0 = (tiles[j] % P.tiles_x) * P.tile_w, y0 = (tiles[j] / P.tiles_x) * P.tile_h;
+            primary += (uint64_t)std::min(P.tile_w, P.img_w - x0) * (uint64_t)std::min(P.tile_h, P.img_h - y0);
+        }
+    } else {
+        primary = (uint64_t)P.img_w * P.img_h;
+    }
+    memset(out, 0, sizeof(*out));
+    cudaError_t ce = cudaSuccess;
+    if (tiles) ce = cudaMemcpyAsync(c->list, tiles, (size_t)ntiles * 4, cudaMemcpyHostToDevice, 0);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(c->cnt, 0, 2 * (size_t)c->max_tiles * 8, 0);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(c->tr.err, 0, 4, 0);
+    if (ce != cudaSuccess) return gcqi::cuda_fail(ce, "rt render setup", __FILE__, __LINE__);
+    const int kind = c->kind;
+    if (!c->fresh) {   // re-initialise the rings this render uses
+        const dim3 ig(64u, (unsigned)std::min(ntiles, 1024));
+        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
+        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
+        else k_init_tiles_sfq<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
+    }
+    c->fresh = false;
     const int TPB = 256;
-    const dim3 grid((unsigned)((threads_per_tile + TPB - 1) / TPB), (unsigned)tiles);
-    unsigned long long* d_alive = d_cnt;
-    unsigned long long* d_traced = d_cnt + tiles;
-    const int ns = (int)sph.size(), nq = (int)quad.size();
-    cudaEventRecord(e0);
-    if (kind == GCQ_GWFQ) k_bgen<GCQ_GWFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
-    else if (kind == GCQ_GLFQ) k_bgen<GCQ_GLFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
-    else k_bgen<GCQ_SFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_rays, d_pix, P, d_alive);
-    cudaEventRecord(e1);
+    const dim3 grid((unsigned)((P.threads_per_tile + TPB - 1) / TPB), (unsigned)ntiles);
+    const int32_t* dl = tiles ? c->list : nullptr;
+    unsigned long long* d_alive = c->cnt;
+    unsigned long long* d_traced = c->cnt + c->max_tiles;
+    cudaEventRecord(c->e0);
+    if (kind == GCQ_GWFQ) k_bgen<GCQ_GWFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
+    else if (kind == GCQ_GLFQ) k_bgen<GCQ_GLFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
+    else k_bgen<GCQ_SFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
+    cudaEventRecord(c->e1);
     if (kind == GCQ_GWFQ)
-        k_btrace<GCQ_GWFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
-                                          d_traced, tr.err);
+        k_btrace<GCQ_GWFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
+                                          c->img, P, d_alive, d_traced, c->tr.err);
     else if (kind == GCQ_GLFQ)
-        k_btrace<GCQ_GLFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
-                                          d_traced, tr.err);
+        k_btrace<GCQ_GLFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
+                                          c->img, P, d_alive, d_traced, c->tr.err);
     else
-        k_btrace<GCQ_SFQ><<<grid, TPB>>>(tr.dq, tr.stride, d_sph, ns, d_quad, nq, d_rays, d_pix, d_img, P, d_alive,
-                                         d_traced, tr.err);
-    cudaEventRecord(e2);
+        k_btrace<GCQ_SFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
+                                         c->img, P, d_alive, d_traced, c->tr.err);
+    cudaEventRecord(c->e2);
     ce = cudaGetLastError();
-    if (ce == cudaSuccess) ce = cudaEventSynchronize(e2);
-    if (ce != cudaSuccess) return fail(ce, "rt bounce kernels");
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(c->e2);
+    if (ce != cudaSuccess) return gcqi::cuda_fail(ce, "rt bounce kernels", __FILE__, __LINE__);
     float gen_ms = 0, trace_ms = 0;
-    cudaEventElapsedTime(&gen_ms, e0, e1);
-    cudaEventElapsedTime(&trace_ms, e1, e2);
-    std::vector<unsigned long long> cnt(2 * (size_t)tiles);
+    cudaEventElapsedTime(&gen_ms, c->e0, c->e1);
+    cudaEventElapsedTime(&trace_ms, c->e1, c->e2);
+    std::vector<unsigned long long> cnt(2 * (size_t)ntiles);
     uint32_t err = 0;
-    ce = cudaMemcpy(cnt.data(), d_cnt, 2 * (size_t)tiles * 8, cudaMemcpyDeviceToHost);
-    if (ce == cudaSuccess) ce = cudaMemcpy(&err, tr.err, 4, cudaMemcpyDeviceToHost);
-    if (ce == cudaSuccess && image) ce = cudaMemcpy(image, d_img, npx * 12, cudaMemcpyDeviceToHost);
-    if (ce != cudaSuccess) return fail(ce, "rt bounce results");
+    ce = cudaMemcpy(cnt.data(), c->cnt, (size_t)ntiles * 8, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(cnt.data() + ntiles, c->cnt + c->max_tiles, (size_t)ntiles * 8, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&err, c->tr.err, 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && image) ce = cudaMemcpy(image, c->img, (size_t)P.img_w * P.img_h * 12, cudaMemcpyDeviceToHost);
+    if (ce != cudaSuccess) return gcqi::cuda_fail(ce, "rt bounce results", __FILE__, __LINE__);
     uint64_t leftover = 0, traced = 0;
-    for (int t = 0; t < tiles; ++t) { leftover += cnt[t]; traced += cnt[tiles + t]; }
+    for (int t = 0; t < ntiles; ++t) { leftover += cnt[t]; traced += cnt[ntiles + t]; }
     out->gen_ms = gen_ms;
     out->trace_ms = trace_ms;
     out->total_ms = gen_ms + trace_ms;
-    out->primary_rays = npx;
+    out->primary_rays = primary;
     out->total_rays = traced;
     out->leftover = leftover;
-    cleanup();
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
     return leftover ? GCQ_EDEVICE : GCQ_OK;
+}
+
+// Render a whole benchmark scene in one call (a context over every tile).
+int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
+                         int max_bounces, uint32_t queue_log2, uint64_t seed, float* image, gcq_rt_result* out) {
+    if (!out) return GCQ_EINVAL;
+    gcq_rt_ctx* c = nullptr;
+    int rc = gcq_rt_ctx_create(kind, scene, width, height, tile_px, threads_per_tile, max_bounces, queue_log2, seed,
+                               0, &c);
+    if (rc != GCQ_OK) return rc;
+    rc = gcq_rt_ctx_render(c, nullptr, 0, image, out);
+    gcq_rt_ctx_destroy(c);
+    return rc;
 }
 
 }  // extern "C"

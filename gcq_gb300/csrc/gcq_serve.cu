@@ -23,13 +23,21 @@
 //              cleanup items that fold a checksum of the levels and reset them; the
 //              last sweep publishes the result and returns the slot
 // Vertices of degree > 32 and cleanup sweeps are processed by the whole warp.
+//
+// Ray tiles of the benchmark scenes (gcq_rt_bounce_render's scenes) are served by
+// the same kernel and worklist: a tile request takes a slot of its scene (ray and
+// path storage for one tile) and worklist room for one item per pixel; a warp
+// writes the tile's primary rays and queues one item per pixel; an item traces one
+// bounce of its pixel's path and re-queues itself while the path continues; the
+// tile's pending count reaching zero schedules one sweep that folds a checksum of
+// the tile's pixels and returns the slot.  The pixels equal gcq_rt_bounce_render's.
 // Every wait is bounded: a full worklist or an idle loop gives up after the
 // configured timeout and reports through the control block's error word.
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
-#include "gcq_internal.cuh"
+#include "gcq_scene.cuh"
 
 namespace {
 
@@ -38,7 +46,9 @@ using gcq::gwf::mpmc;
 constexpr uint32_t UNVISITED = 0x7F7F7F7Fu;   // byte-settable, above any level
 constexpr uint32_t SLOT_BITS = 14, LVL_BITS = 18;
 constexpr uint32_t CLEANUP = (1u << LVL_BITS) - 1;    // level field of a sweep item
-constexpr uint32_t MAX_LEVEL = CLEANUP - 1;
+constexpr uint32_t RAY = CLEANUP - 1;                 // level field of a ray item (vertex field: pixel in tile)
+constexpr uint32_t RAY_GEN = CLEANUP - 2;             // level field of a tile's generation item
+constexpr uint32_t MAX_LEVEL = CLEANUP - 3;
 constexpr uint32_t MAX_SLOTS = 1u << SLOT_BITS;
 constexpr uint32_t SWEEP = 1u << 13;                  // vertices per sweep item
 constexpr int WARP_DEG = 32;
@@ -57,11 +67,23 @@ constexpr uint32_t POLL_TRIES = 2;    // fast-path attempts per poll of a server
 // wait-free slow path is not entered in practice (see gcq_serve_default_cfg).
 constexpr uint32_t SERVER_PATIENCE = 1u << 16;
 
+// A scene served as tiles: the renderer's parameters and geometry, and the image.
+struct srv_scene {
+    bparams P;
+    const BSphere* sph;
+    const BQuad* quad;
+    float* img;
+    int32_t ns, nq, tiles, _pad;
+};
+
+// A target of requests: a graph (scene == nullptr) or a scene.  For a scene, V is
+// the pixels of a tile (its worklist reservation) and sweeps is 1.
 struct srv_graph {
     const int32_t* off;
     const int32_t* idx;
-    mpmc* subq;        // submitted requests of this graph (request index)
-    mpmc* slotq;       // free slots of this graph (global slot index)
+    mpmc* subq;        // submitted requests of this target (request index)
+    mpmc* slotq;       // free slots of this target (global slot index)
+    const srv_scene* scene;
     int32_t V;
     uint32_t slot0, nslots, sweeps;
 };
@@ -76,10 +98,12 @@ struct alignas(128) srv_slot {
     gcq::u32a max_level;
     gcq::u32a sweeps_left;
     int32_t req;
-    int32_t graph;
-    int32_t _pad;
+    int32_t graph;          // target index
+    int32_t src;            // tile index of a tile request
     uint64_t done_ns;
     int32_t* level;         // UNVISITED everywhere while the slot is free
+    BRay* rays;             // a tile slot's rays and path states, one per pixel
+    BPix* pix;
 };
 
 struct alignas(128) srv_ctl {
@@ -98,9 +122,11 @@ struct alignas(128) srv_ctl {
     uint32_t ngraphs;
     uint32_t _pad;
     gcq::u64a stat[4];        // items, stale items, edges scanned, sweeps
+    gcq::u64a stat2[4];       // rays traced
 };
 
 enum { ST_ITEMS, ST_STALE, ST_EDGES, ST_SWEEPS };
+enum { ST_RAYS = 0 };   // index into srv_ctl::stat2
 
 struct srv_ctx {
     mpmc* workq;
@@ -122,6 +148,12 @@ __device__ __forceinline__ uint32_t item_v(uint64_t x) { return (uint32_t)x; }
 // splitmix64(v << 32 | level(v)), level 0xFFFFFFFF for unreached vertices.
 __device__ __forceinline__ uint64_t level_term(uint32_t v, uint32_t lvl) {
     return gcqi::splitmix64(((uint64_t)v << 32) | lvl);
+}
+
+// Checksum of a tile: sum (mod 2^64) over its pixels g (row-major in the image) and
+// channels c of splitmix64((3g + c) << 32 | bits of the channel's float).
+__device__ __forceinline__ uint64_t pixel_term(uint32_t g, int c, float v) {
+    return gcqi::splitmix64(((uint64_t)(3u * g + (uint32_t)c) << 32) | (uint64_t)__float_as_uint(v));
 }
 
 __device__ __forceinline__ uint64_t now_ns(const srv_ctx& x) {
@@ -210,24 +242,52 @@ __device__ __noinline__ void control(const srv_ctx& x, uint32_t ctid, uint32_t t
         const int32_t src = x.reqs[r].src;
         s->req = (int32_t)r;
         s->graph = (int32_t)gi;
+        s->src = src;
         gcq::st_rlx(&s->checksum, 0ull);
         gcq::st_rlx(&s->reached, 0u);
         gcq::st_rlx(&s->max_level, 0u);
         gcq::st_rlx(&s->pending, 1ull);
-        s->level[src] = 0;
         x.res[r].admit_ns = now_ns(x);
-        push_item(x, pack_item((uint32_t)slot, 0, (uint32_t)src), ctid << 5);   // release publishes the slot
+        if (g.scene) {
+            push_item(x, pack_item((uint32_t)slot, RAY_GEN, 0), ctid << 5);   // release publishes the slot
+        } else {
+            s->level[src] = 0;
+            push_item(x, pack_item((uint32_t)slot, 0, (uint32_t)src), ctid << 5);
+        }
         ++admitted;
     }
 }
 
-__global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
+// One bounce of the path of pixel `i` of the tile in `slot`: the item re-queues
+// itself while the path continues; a finished path writes its pixel, adds its rays
+// to the tile's count and settles the item.
+__device__ __noinline__ void serve_ray(const srv_ctx& x, uint64_t it, uint32_t slot, uint32_t i, uint32_t tid) {
+    srv_slot* s = &x.slots[slot];
+    const srv_scene* sc = x.graphs[s->graph].scene;
+    BRay r = s->rays[i];
+    BPix st = s->pix[i];
+    const BHit hit = btrace(r, sc->sph, sc->ns, sc->quad, sc->nq);
+    V3 c;
+    if (bshade(r, st, hit, sc->P, &c)) {
+        s->rays[i] = r;
+        s->pix[i] = st;
+        push_item(x, it, tid);   // the child inherits the item's count
+        return;
+    }
+    float* o = sc->img + 3 * (size_t)r.pix;
+    o[0] = c.x; o[1] = c.y; o[2] = c.z;
+    atomicAdd((unsigned int*)&s->reached, r.depth + 1);
+    atomicMax((unsigned int*)&s->max_level, r.depth + 1);
+    settle(x, slot, 0, tid);
+}
+
+__global__ void __launch_bounds__(256, 3) k_serve(srv_ctx x) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t ctid = tid >> 5;
     const int lane = (int)(threadIdx.x & 31);
     srv_ctl* c = x.ctl;
     const uint32_t nreq = c->nreq;
-    uint64_t n_items = 0, n_stale = 0, n_edges = 0, n_sweeps = 0;
+    uint64_t n_items = 0, n_stale = 0, n_edges = 0, n_sweeps = 0, n_rays = 0;
     // stall detection: progress is any enqueue on the worklist (its Tail counter) or
     // a completion; one thread going without an item proves nothing
     uint64_t idle_since = 0, idle_mark = 0;
@@ -249,7 +309,9 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
         // them two loads, not a Head ticket and a marked slot each
         const bool got = gcq::gwf::maybe_nonempty(&x.workq->aq) &&
                          gcq::gwf::try_dequeue_ptr(x.workq, &it, tid, POLL_TRIES);
-        int big = 0;   // 1: an edge range of one vertex (lvl = the level it gives), 2: a cleanup sweep
+        // 1: an edge range of one vertex (lvl = the level it gives), 2: a cleanup sweep,
+        // 3: a tile's primary rays
+        int big = 0;
         uint32_t slot = 0, lvl = 0, v = 0;
         int rb = 0, re = 0;
         if (got) {
@@ -258,6 +320,11 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
             v = item_v(it);
             if (lvl == CLEANUP) {
                 big = 2;
+            } else if (lvl == RAY) {
+                ++n_rays;
+                serve_ray(x, it, slot, v, tid);
+            } else if (lvl == RAY_GEN) {
+                big = 3;
             } else if (v & CHUNK_BIT) {
                 ++n_items;
                 srv_slot* s = &x.slots[slot];
@@ -326,7 +393,29 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
             srv_slot* s = &x.slots[os];
             const srv_graph& g = x.graphs[s->graph];
             int32_t* level = s->level;
-            if (kind == 1) {
+            if (kind == 3) {
+                // primary rays of the tile, one item per pixel
+                const srv_scene* sc = g.scene;
+                const bparams& P = sc->P;
+                const int tile = s->src;
+                const int x0 = (tile % P.tiles_x) * P.tile_w, y0 = (tile / P.tiles_x) * P.tile_h;
+                const int tw = min(P.tile_w, P.img_w - x0), th = min(P.tile_h, P.img_h - y0);
+                const int npx = tw * th;
+                // count the children before any of them can be dequeued
+                if (lane == owner) gcq::fetch_add(&s->pending, (uint64_t)npx);
+                __syncwarp();
+                for (int i = lane; i < npx; i += 32) {
+                    const int px = x0 + i % tw, py = y0 + i / tw;
+                    BRay r;
+                    BPix st;
+                    bprimary(P, px, py, (uint32_t)(py * P.img_w + px), &r, &st);
+                    s->rays[i] = r;
+                    s->pix[i] = st;
+                    push_item(x, pack_item(os, RAY, (uint32_t)i), tid);
+                }
+                __syncwarp();
+                if (lane == owner) settle(x, os, 0, tid);
+            } else if (kind == 1) {
                 const uint32_t lv = ol;   // the level this range's neighbours get
                 if (lane == owner) n_edges += (uint64_t)(end - beg);
                 if (lv > MAX_LEVEL) {
@@ -349,18 +438,32 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
                 }
                 if (lane == owner) settle(x, os, 0, tid);
             } else {
-                // sweep ov: checksum and reset vertices [ov * SWEEP, +SWEEP)
-                const uint32_t lo = ov * SWEEP;
-                const uint32_t hi = min((uint32_t)g.V, lo + SWEEP);
                 uint64_t sum = 0;
                 uint32_t reached = 0, maxl = 0;
-                for (uint32_t u = lo + (uint32_t)lane; u < hi; u += 32) {
-                    const uint32_t l = (uint32_t)level[u];
-                    const bool r = (l != UNVISITED);
-                    sum += level_term(u, r ? l : 0xFFFFFFFFu);
-                    reached += r ? 1u : 0u;
-                    maxl = (r && l > maxl) ? l : maxl;
-                    level[u] = (int32_t)UNVISITED;
+                if (g.scene) {
+                    // a finished tile: checksum of its pixels (rays and path lengths are
+                    // already counted)
+                    const bparams& P = g.scene->P;
+                    const float* img = g.scene->img;
+                    const int tile = s->src;
+                    const int x0 = (tile % P.tiles_x) * P.tile_w, y0 = (tile / P.tiles_x) * P.tile_h;
+                    const int tw = min(P.tile_w, P.img_w - x0), th = min(P.tile_h, P.img_h - y0);
+                    for (int i = lane; i < tw * th; i += 32) {
+                        const uint32_t px = (uint32_t)((y0 + i / tw) * P.img_w + (x0 + i % tw));
+                        for (int ch = 0; ch < 3; ++ch) sum += pixel_term(px, ch, img[3 * (size_t)px + ch]);
+                    }
+                } else {
+                    // sweep ov: checksum and reset vertices [ov * SWEEP, +SWEEP)
+                    const uint32_t lo = ov * SWEEP;
+                    const uint32_t hi = min((uint32_t)g.V, lo + SWEEP);
+                    for (uint32_t u = lo + (uint32_t)lane; u < hi; u += 32) {
+                        const uint32_t l = (uint32_t)level[u];
+                        const bool r = (l != UNVISITED);
+                        sum += level_term(u, r ? l : 0xFFFFFFFFu);
+                        reached += r ? 1u : 0u;
+                        maxl = (r && l > maxl) ? l : maxl;
+                        level[u] = (int32_t)UNVISITED;
+                    }
                 }
                 for (int o = 16; o > 0; o >>= 1) {
                     sum += __shfl_xor_sync(FULL, sum, o);
@@ -411,12 +514,14 @@ __global__ void __launch_bounds__(256) k_serve(srv_ctx x) {
         n_stale += __shfl_xor_sync(FULL, n_stale, o);
         n_edges += __shfl_xor_sync(FULL, n_edges, o);
         n_sweeps += __shfl_xor_sync(FULL, n_sweeps, o);
+        n_rays += __shfl_xor_sync(FULL, n_rays, o);
     }
     if (lane == 0) {
         gcq::fetch_add_rlx(&c->stat[ST_ITEMS], n_items);
         gcq::fetch_add_rlx(&c->stat[ST_STALE], n_stale);
         gcq::fetch_add_rlx(&c->stat[ST_EDGES], n_edges);
         gcq::fetch_add_rlx(&c->stat[ST_SWEEPS], n_sweeps);
+        if (n_rays) gcq::fetch_add_rlx(&c->stat2[ST_RAYS], n_rays);
     }
 }
 
@@ -450,7 +555,11 @@ uint32_t log2_ceil(uint64_t n) {
 }  // namespace
 
 struct gcq_server {
-    std::vector<srv_graph> graphs;
+    std::vector<srv_graph> graphs;     // targets: the graphs, then the scenes
+    int ngraphs = 0, nscenes = 0;
+    std::vector<float*> scene_img;
+    std::vector<uint64_t> scene_px;
+    std::vector<int32_t> scene_tiles;
     std::vector<void*> dev;            // device allocations
     std::vector<gcq_queue*> queues;    // workq first, then subq/slotq per graph
     srv_graph* d_graphs = nullptr;
@@ -498,13 +607,27 @@ void gcq_serve_default_cfg(gcq_serve_cfg* c) {
     c->work_knobs.deq_patience = SERVER_PATIENCE;
     c->threads = 0;
     c->work_log2 = 0;
+    c->rt_scenes = 0;
+    c->rt_width = c->rt_height = 1024;
+    c->rt_tile_px = 32;
+    c->rt_max_bounces = 4;
+    c->rt_slots = 1024;
+    c->rt_seed = 1;
 }
 
 int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* const* indices,
                      const int32_t* V, const int64_t* E, const gcq_serve_cfg* cfg, gcq_server** out) {
     if (!out) return GCQ_EINVAL;
     *out = nullptr;
-    if (ngraphs <= 0 || ngraphs > MAX_GRAPHS || !offsets || !indices || !V || !E || !cfg) return GCQ_EINVAL;
+    if (!cfg || ngraphs < 0 || ngraphs > MAX_GRAPHS || (ngraphs > 0 && (!offsets || !indices || !V || !E)))
+        return GCQ_EINVAL;
+    if (ngraphs == 0 && cfg->rt_scenes == 0) return GCQ_EINVAL;
+    if (cfg->rt_scenes > 2) return GCQ_EINVAL;
+    if (cfg->rt_scenes && (cfg->rt_width == 0 || cfg->rt_height == 0 || cfg->rt_tile_px == 0 ||
+                           cfg->rt_tile_px > 256 || cfg->rt_max_bounces > 1000 || cfg->rt_slots == 0 ||
+                           (uint64_t)cfg->rt_width * cfg->rt_height > (1ull << 30)))
+        return GCQ_EINVAL;
+    if (ngraphs + (int)cfg->rt_scenes > MAX_GRAPHS) return GCQ_EINVAL;
     gcq_server* s = new gcq_server();
     auto fail = [&](int r) { delete s; return r; };
     int rc = GCQ_OK;
@@ -527,9 +650,10 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
     s->timeout_ns = cfg->timeout_ns ? cfg->timeout_ns : 10000000000ull;
     s->run_limit_ns = cfg->run_limit_ns ? cfg->run_limit_ns : 60000000000ull;
     // slot pools: an even share of the budget per graph, at most max_slots each
+    const uint32_t ntargets = (uint32_t)ngraphs + cfg->rt_scenes;
     const uint32_t per_graph_cap =
-        std::min<uint32_t>(cfg->max_slots ? cfg->max_slots : 1024, MAX_SLOTS / (uint32_t)ngraphs);
-    const uint64_t share = cfg->budget_bytes / (uint64_t)ngraphs;
+        std::min<uint32_t>(cfg->max_slots ? cfg->max_slots : 1024, MAX_SLOTS / ntargets);
+    const uint64_t share = cfg->budget_bytes / (uint64_t)ntargets;
     uint64_t level_elems = 0;
     uint32_t ctl_threads = (uint32_t)(threads / 32);
     for (int g = 0; g < ngraphs; ++g) {
@@ -545,6 +669,66 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
         level_elems += (uint64_t)n * (uint64_t)V[g];
         ctl_threads = std::max(ctl_threads, n);
         s->graphs.push_back(hg);
+    }
+    // scenes: a tile slot holds a 32-byte ray and a 16-byte path state per pixel
+    const uint32_t tile_px2 = cfg->rt_tile_px * cfg->rt_tile_px;
+    uint64_t tile_elems = 0;
+    for (uint32_t sc = 0; sc < cfg->rt_scenes; ++sc) {
+        const uint64_t bytes = (uint64_t)tile_px2 * (sizeof(BRay) + sizeof(BPix));
+        const uint32_t n = (uint32_t)std::min<uint64_t>(std::min<uint32_t>(cfg->rt_slots, MAX_SLOTS / ntargets),
+                                                        share / bytes);
+        if (n == 0) return fail(GCQ_ECAPACITY);
+        srv_graph hg{};
+        hg.V = (int32_t)tile_px2;
+        hg.slot0 = s->total_slots;
+        hg.nslots = n;
+        hg.sweeps = 1;
+        s->total_slots += n;
+        tile_elems += (uint64_t)n * tile_px2;
+        ctl_threads = std::max(ctl_threads, n);
+        s->graphs.push_back(hg);
+        maxV = std::max(maxV, (int32_t)tile_px2);
+    }
+    s->ngraphs = ngraphs;
+    s->nscenes = (int)cfg->rt_scenes;
+    for (uint32_t sc = 0; sc < cfg->rt_scenes; ++sc) {
+        srv_scene hs{};
+        memset(&hs, 0, sizeof hs);
+        bparams& P = hs.P;
+        P.img_w = (int)cfg->rt_width;
+        P.img_h = (int)cfg->rt_height;
+        P.tile_w = P.tile_h = (int)cfg->rt_tile_px;
+        P.tiles_x = (P.img_w + P.tile_w - 1) / P.tile_w;
+        P.threads_per_tile = 0;
+        P.max_depth = (int)cfg->rt_max_bounces;
+        P.seed = cfg->rt_seed;
+        std::vector<BSphere> sph;
+        std::vector<BQuad> quad;
+        build_bscene((int)sc, cfg->rt_seed, sph, quad, P);
+        hs.ns = (int32_t)sph.size();
+        hs.nq = (int32_t)quad.size();
+        hs.tiles = P.tiles_x * ((P.img_h + P.tile_h - 1) / P.tile_h);
+        BSphere* d_sph = nullptr;
+        BQuad* d_quad = nullptr;
+        float* d_img = nullptr;
+        srv_scene* d_sc = nullptr;
+        const size_t img_bytes = (size_t)P.img_w * P.img_h * 12;
+        if ((rc = dev_alloc(s, &d_sph, std::max<size_t>(1, sph.size()) * sizeof(BSphere))) != GCQ_OK ||
+            (rc = dev_alloc(s, &d_quad, std::max<size_t>(1, quad.size()) * sizeof(BQuad))) != GCQ_OK ||
+            (rc = dev_alloc(s, &d_img, img_bytes)) != GCQ_OK || (rc = dev_alloc(s, &d_sc, sizeof(srv_scene))) != GCQ_OK)
+            return fail(rc);
+        hs.sph = d_sph;
+        hs.quad = d_quad;
+        hs.img = d_img;
+        if ((!sph.empty() && cudaMemcpy(d_sph, sph.data(), sph.size() * sizeof(BSphere), cudaMemcpyHostToDevice) != cudaSuccess) ||
+            (!quad.empty() && cudaMemcpy(d_quad, quad.data(), quad.size() * sizeof(BQuad), cudaMemcpyHostToDevice) != cudaSuccess) ||
+            cudaMemset(d_img, 0, img_bytes) != cudaSuccess ||
+            cudaMemcpy(d_sc, &hs, sizeof hs, cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(gcqi::cuda_fail(cudaGetLastError(), "scene upload", __FILE__, __LINE__));
+        s->graphs[ngraphs + sc].scene = d_sc;
+        s->scene_img.push_back(d_img);
+        s->scene_px.push_back((uint64_t)P.img_w * P.img_h);
+        s->scene_tiles.push_back(hs.tiles);
     }
     // graphs
     for (int g = 0; g < ngraphs; ++g) {
@@ -571,7 +755,7 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
     if ((rc = gcq_create(GCQ_GWFQ, work_log2, s->threads, &cfg->work_knobs, &q)) != GCQ_OK) return fail(rc);
     s->queues.push_back(q);
     const uint32_t ctl_log2 = std::max<uint32_t>(log2_ceil(ctl_threads), 10);
-    for (int g = 0; g < ngraphs; ++g) {
+    for (uint32_t g = 0; g < ntargets; ++g) {
         const uint32_t sub_log2 = std::max<uint32_t>(ctl_log2, 16);
         if ((rc = gcq_create(GCQ_GWFQ, sub_log2, ctl_threads, &k, &q)) != GCQ_OK) return fail(rc);
         s->queues.push_back(q);
@@ -582,24 +766,45 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
         s->queues.push_back(q);
         s->graphs[g].slotq = (mpmc*)q->obj;
     }
-    if ((rc = dev_alloc(s, &s->d_graphs, sizeof(srv_graph) * ngraphs)) != GCQ_OK) return fail(rc);
-    if (cudaMemcpy(s->d_graphs, s->graphs.data(), sizeof(srv_graph) * ngraphs, cudaMemcpyHostToDevice) != cudaSuccess)
+    if ((rc = dev_alloc(s, &s->d_graphs, sizeof(srv_graph) * ntargets)) != GCQ_OK) return fail(rc);
+    if (cudaMemcpy(s->d_graphs, s->graphs.data(), sizeof(srv_graph) * ntargets, cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(gcqi::cuda_fail(cudaGetLastError(), "graph table", __FILE__, __LINE__));
     // level arrays (UNVISITED) and slot headers
     s->level_bytes = level_elems * 4;
-    if ((rc = dev_alloc(s, &s->d_levels, (size_t)s->level_bytes)) != GCQ_OK) return fail(rc);
+    if ((rc = dev_alloc(s, &s->d_levels, (size_t)std::max<uint64_t>(s->level_bytes, 4))) != GCQ_OK) return fail(rc);
     if (cudaMemset(s->d_levels, 0x7F, (size_t)s->level_bytes) != cudaSuccess)
         return fail(gcqi::cuda_fail(cudaGetLastError(), "level reset", __FILE__, __LINE__));
+    BRay* d_rays = nullptr;
+    BPix* d_pix = nullptr;
+    if (tile_elems) {
+        if ((rc = dev_alloc(s, &d_rays, tile_elems * sizeof(BRay))) != GCQ_OK ||
+            (rc = dev_alloc(s, &d_pix, tile_elems * sizeof(BPix))) != GCQ_OK)
+            return fail(rc);
+    }
     std::vector<srv_slot> hs(s->total_slots);
     memset((void*)hs.data(), 0, sizeof(srv_slot) * hs.size());
-    uint64_t off = 0;
-    for (const srv_graph& g : s->graphs)
-        for (uint32_t i = 0; i < g.nslots; ++i, off += (uint64_t)g.V) hs[g.slot0 + i].level = s->d_levels + off;
+    uint64_t off = 0, toff = 0;
+    for (const srv_graph& g : s->graphs) {
+        if (g.scene) {
+            for (uint32_t i = 0; i < g.nslots; ++i, toff += (uint64_t)g.V) {
+                hs[g.slot0 + i].rays = d_rays + toff;
+                hs[g.slot0 + i].pix = d_pix + toff;
+            }
+        } else {
+            for (uint32_t i = 0; i < g.nslots; ++i, off += (uint64_t)g.V) hs[g.slot0 + i].level = s->d_levels + off;
+        }
+    }
     if ((rc = dev_alloc(s, &s->d_slots, sizeof(srv_slot) * hs.size())) != GCQ_OK) return fail(rc);
     if (cudaMemcpy(s->d_slots, hs.data(), sizeof(srv_slot) * hs.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(gcqi::cuda_fail(cudaGetLastError(), "slot table", __FILE__, __LINE__));
     if ((rc = dev_alloc(s, &s->d_ctl, sizeof(srv_ctl))) != GCQ_OK) return fail(rc);
     *out = s;
+    return GCQ_OK;
+}
+
+int gcq_serve_image(const gcq_server* s, int scene, float* image) {
+    if (!s || !image || scene < 0 || scene >= s->nscenes) return GCQ_EINVAL;
+    GCQ_CUDA(cudaMemcpy(image, s->scene_img[scene], s->scene_px[scene] * 12, cudaMemcpyDeviceToHost));
     return GCQ_OK;
 }
 
@@ -625,7 +830,8 @@ int gcq_serve_run(gcq_server* s, const gcq_serve_req* reqs, uint32_t nreq, gcq_s
     for (uint32_t i = 0; i < nreq; ++i) {
         const int g = reqs[i].graph;
         if (g < 0 || g >= (int)s->graphs.size()) return GCQ_EINVAL;
-        if (reqs[i].src < 0 || reqs[i].src >= s->graphs[g].V) return GCQ_EINVAL;
+        const int32_t lim = g < s->ngraphs ? s->graphs[g].V : s->scene_tiles[g - s->ngraphs];
+        if (reqs[i].src < 0 || reqs[i].src >= lim) return GCQ_EINVAL;
         if (i && reqs[i].arrival_ns < reqs[i - 1].arrival_ns) return GCQ_EINVAL;   // sorted by arrival
         if (reqs[i].arrival_ns > MAX_ARRIVAL_NS) return GCQ_EINVAL;
     }
@@ -709,6 +915,7 @@ int gcq_serve_run(gcq_server* s, const gcq_serve_req* reqs, uint32_t nreq, gcq_s
         stats->stale = hc.stat[ST_STALE];
         stats->edges = hc.stat[ST_EDGES];
         stats->sweeps = hc.stat[ST_SWEEPS];
+        stats->rays = hc.stat2[ST_RAYS];
         stats->completed = hc.completed;
         stats->error_word = err;
         stats->released = hc.next_release;

@@ -322,6 +322,19 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
 int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
                          int max_bounces, uint32_t queue_log2, uint64_t seed, float* image, gcq_rt_result* out);
 
+/* The same renderer as a context that renders lists of tiles, for callers that
+ * render a tile at a time (one launch per tile request).  Rings, ray storage for
+ * up to max_tiles tiles (<= 0: every tile) and the device image are allocated
+ * once; gcq_rt_ctx_render renders the listed row-major tile indices (tiles NULL:
+ * all, which needs max_tiles <= 0) into the image and copies the whole image to
+ * `image` when it is not NULL.  A tile's pixels are the same whichever list
+ * renders it. */
+typedef struct gcq_rt_ctx gcq_rt_ctx;
+int gcq_rt_ctx_create(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
+                      int max_bounces, uint32_t queue_log2, uint64_t seed, int max_tiles, gcq_rt_ctx** out);
+int gcq_rt_ctx_render(gcq_rt_ctx* ctx, const int32_t* tiles, int ntiles, float* image, gcq_rt_result* out);
+int gcq_rt_ctx_destroy(gcq_rt_ctx* ctx);
+
 /* The stream-compaction baseline (concurrent_rt/baselines/rt_compaction.cpp): the
  * same scenes (plus its scene 2, the mirror tunnel, which gcq_rt_render also
  * accepts), double-buffered ray lists packed in order after every pass, its own
@@ -375,21 +388,30 @@ typedef struct gcq_serve_cfg {
     uint64_t run_limit_ns;  /* a run gives up (GCQ_ETIMEDOUT) this long after the last
                                arrival; default 60 s */
     gcq_knobs work_knobs;   /* knobs of the worklist queue; default gcq_default_knobs */
+    /* Ray tiles (gcq_rt_bounce_render's scenes): rt_scenes > 0 serves tile requests of
+     * scenes 0 .. rt_scenes-1 as targets ngraphs + scene.  Default 0 (none); the
+     * other fields default to the benchmark image (1024 x 1024, 32-pixel tiles,
+     * 4 bounces, seed 1) and 1024 tile slots per scene. */
+    uint32_t rt_scenes;
+    uint32_t rt_width, rt_height, rt_tile_px, rt_max_bounces, rt_slots;
+    uint64_t rt_seed;
 } gcq_serve_cfg;
 
 typedef struct gcq_serve_req {
-    int32_t graph;          /* index into the graphs given to gcq_serve_create */
-    int32_t src;            /* source vertex */
+    int32_t graph;          /* target: a graph given to gcq_serve_create, or
+                               ngraphs + scene for a ray tile */
+    int32_t src;            /* source vertex, or the tile's row-major index */
     uint64_t arrival_ns;    /* release time (<= 60 s); requests are sorted by it */
 } gcq_serve_req;
 
 typedef struct gcq_serve_res {
     uint64_t admit_ns;      /* slot granted */
-    uint64_t done_ns;       /* last vertex settled */
+    uint64_t done_ns;       /* last vertex settled / last path of the tile ended */
     uint64_t finish_ns;     /* checksum folded, slot returned (response time) */
-    uint64_t checksum;
-    uint32_t reached;
-    int32_t max_level;
+    uint64_t checksum;      /* traversal: see gcq_serve_run; tile: sum over its pixels g
+                               and channels c of splitmix64((3g + c) << 32 | float bits) */
+    uint32_t reached;       /* vertices reached; tile: rays traced */
+    int32_t max_level;      /* eccentricity of the source; tile: longest path in rays */
 } gcq_serve_res;
 
 typedef struct gcq_serve_stats {
@@ -406,6 +428,7 @@ typedef struct gcq_serve_stats {
     uint64_t work_tail[2];  /* ticket counters of the worklist's rings at the end: */
     uint64_t work_head[2];  /*   [0] the item ring, [1] the free-index ring */
     int32_t work_threshold[2];
+    uint64_t rays;          /* ray items traced (tile requests) */
 } gcq_serve_stats;
 
 void gcq_serve_default_cfg(gcq_serve_cfg* cfg);
@@ -422,6 +445,9 @@ int gcq_serve_info(const gcq_server* s, int graph, uint32_t* slots, uint32_t* th
  * res[i] answers reqs[i].  Synchronises the device. */
 int gcq_serve_run(gcq_server* s, const gcq_serve_req* reqs, uint32_t nreq, gcq_serve_res* res,
                   gcq_serve_stats* stats);
+/* Copy the image of a served scene (rt_width * rt_height RGB floats): every pixel
+ * of a tile served so far equals gcq_rt_bounce_render's. */
+int gcq_serve_image(const gcq_server* s, int scene, float* image);
 
 #ifdef __cplusplus
 }

@@ -138,3 +138,78 @@ def test_serve_rejects(gcq, graphs):
     with pytest.raises(gcq.GcqError) as e:
         gcq.Server(graphs[:1], budget_bytes=16)       # not one level array fits
     assert e.value.status == gcq.ECAPACITY
+
+
+# ---------------------------------------------------------------- ray tiles
+def _bounce_image(oracle_lib, scene, w, h, bounces=4, seed=1):
+    img = np.zeros((h, w, 3), np.float32)
+    n = oracle_lib.lib().oracle_rt_bounce_render(scene, w, h, bounces, seed, 16, img.ctypes.data)
+    return img, n
+
+
+def _check_tiles(gcq, res, reqs, ngraphs, images, tile_px=32):
+    for i in range(len(reqs)):
+        tgt = int(reqs[i]["graph"])
+        if tgt < ngraphs:
+            continue
+        want = gcq.tile_checksum(images[tgt - ngraphs], int(reqs[i]["src"]), tile_px)
+        assert int(res[i]["checksum"]) == want, (i, reqs[i])
+        assert res[i]["reached"] >= (tile_px * tile_px) and res[i]["max_level"] >= 1
+        assert res[i]["admit_ns"] <= res[i]["done_ns"] <= res[i]["finish_ns"]
+
+
+def test_serve_tiles_full_image(gcq, oracle_lib):
+    """Every 32x32 tile of both 1024x1024 scenes as a request, no graphs: the served
+    images equal the serial renders bit for bit, each tile's checksum matches, and
+    the tiles' ray counts add up to the render's."""
+    images = [_bounce_image(oracle_lib, s, 1024, 1024) for s in (0, 1)]
+    reqs = np.zeros(2048, dtype=gcq.SERVE_REQ_DTYPE)
+    reqs["graph"] = np.repeat([0, 1], 1024)
+    reqs["src"] = np.tile(np.arange(1024), 2)
+    with gcq.Server([], rt_scenes=2, threads=65536, **LIMITS) as s:
+        res, st = s.run(reqs)
+        for sc in (0, 1):
+            assert np.array_equal(s.image(sc).view(np.uint32), images[sc][0].view(np.uint32)), sc
+            assert int(res["reached"][reqs["graph"] == sc].sum()) == images[sc][1]
+        _check_tiles(gcq, res, reqs, 0, [im for im, _ in images])
+        assert st["rays"] == images[0][1] + images[1][1]
+        assert st["completed"] == len(reqs) and st["error_word"] == 0
+
+
+def test_serve_mixed_poisson(gcq, oracle_lib, graphs, expected):
+    """Traversals and tiles of both scenes interleaved, open-loop arrivals, few tile
+    slots (reused many times) and a second run on the same server."""
+    images = [_bounce_image(oracle_lib, s, 256, 192, bounces=5, seed=3)[0] for s in (0, 1)]
+    ng = len(graphs)
+    V = [len(o) - 1 for o, _ in graphs]
+    with gcq.Server(graphs, budget_bytes=1 << 30, threads=32768, rt_scenes=2, rt_size=(256, 192),
+                    rt_max_bounces=5, rt_seed=3, rt_slots=8, **LIMITS) as s:
+        assert s.rt_tiles == 48
+        for seed, rate in [(31, 3e4), (32, 0)]:
+            rng = np.random.default_rng(seed)
+            reqs = gcq.serve_requests(400, ng + 2, V + [48, 48], rate_per_s=rate, seed=seed)
+            tiles = reqs["graph"] >= ng
+            reqs["src"][tiles] = rng.integers(0, 48, size=int(tiles.sum()))
+            res, st = s.run(reqs)
+            bfs = ~tiles
+            _check(res[bfs], reqs[bfs], expected)
+            _check_tiles(gcq, res, reqs, ng, images)
+            assert st["completed"] == len(reqs)
+
+
+def test_serve_tiles_reject(gcq, graphs):
+    with gcq.Server(graphs[:1], budget_bytes=1 << 28, threads=4096, rt_scenes=1, **LIMITS) as s:
+        bad = np.zeros(2, dtype=gcq.SERVE_REQ_DTYPE)
+        bad["graph"] = [1, 1]
+        bad["src"] = [0, 1024]                       # tile index out of range
+        with pytest.raises(gcq.GcqError) as e:
+            s.run(bad)
+        assert e.value.status == gcq.EINVAL
+        bad["graph"][1] = 2                          # scene 1 is not served
+        bad["src"][1] = 0
+        with pytest.raises(gcq.GcqError) as e:
+            s.run(bad)
+        assert e.value.status == gcq.EINVAL
+        with pytest.raises(gcq.GcqError) as e:
+            s.image(1)
+        assert e.value.status == gcq.EINVAL
