@@ -20,10 +20,20 @@ chunk launch over all threads.  Metric: successful queue operations per second
 stream of traversal requests over resident graphs -- R-MAT scales 16..22 (edge
 factor 16, a,b,c = 0.57,0.19,0.19) and the two seeded grids (4096^2 and 212^2,
 keep 0.6, diagonals 0.01) -- admitted into a 150 GiB level-array budget and served
-by one persistent kernel.  A step is one run of the whole request set.  Metric:
-traversals per second; latency p50/p99 from arrival to response.  It also times
-one persistent BFS launch per request (gcq_bfs_run) on a sample of the same
-requests, and the oracle's serial BFS on the host.
+by one persistent kernel, mixed with ray-tile requests (--serve-tiles, default
+2048: every 32x32 tile of both 1024x1024 benchmark scenes) served by the same
+kernel.  A step is one run of the whole request set.  Metric: traversals per
+second (tiles per second beside it); latency p50/p99 from arrival to response for
+each kind.  It also times one launch per request -- a persistent gcq_bfs_run per
+traversal, a single-tile gcq_rt_ctx_render per tile -- on a sample of the same
+requests, and the oracle's serial BFS and render on the host.
+
+--workload rt renders the two benchmark scenes with the ray-bounce queues: 1024x1024
+pixels, 1 sample per pixel, at most 4 bounces, 32x32-pixel tiles with 1024 threads
+and a 2^15 G-WFQ ring each, 32-byte rays.  A step is one frame of each scene
+(gcq_rt_ctx_render over all tiles); metric: rays traced per second (MRays/s).  The
+roofline is the unfused fp32 rate measured in the same run (the renderer is built
+without multiply-add contraction); the CPU baseline is the oracle's serial render.
 
 --impl reference runs the reference algorithm on the host cores instead: the
 reference is HIP for AMD GPUs and cannot run here, so its arm is the oracle's CPU
@@ -317,7 +327,116 @@ def run_gpu(args):
     return 0
 
 
-SERVE_METRIC = "served BFS traversals/s (RMAT 16..22 + grids A, B)"
+SERVE_METRIC = "served BFS traversals/s (RMAT 16..22 + grids A, B, mixed with ray tiles)"
+RT_METRIC = "RT MRays/s (ray-bounce queue, 1024x1024, 1 spp, 4 bounces, scenes 0 and 1)"
+RT_SIZE, RT_TILE, RT_TPT, RT_BOUNCES, RT_QLOG2, RT_SEED = 1024, 32, 1024, 4, 15, 1
+
+
+def rt_flops_per_ray(spheres, quads):
+    """Algorithmic fp32 operations of one ray: 20 per sphere test, 12 per quad test,
+    60 for the shading."""
+    return 20 * spheres + 12 * quads + 60
+
+
+RT_SCENE_PRIMS = {0: (512, 1), 1: (0, 17)}   # spheres, quads of each benchmark scene
+
+
+def run_rt(args):
+    """The benchmark scenes: one frame of each per step."""
+    import numpy as np
+    import torch
+    import gcq_gb300 as g
+    from oracle import build as obuild, lib as olib
+
+    rank, world, local = _env_rank()
+    if rank != 0:
+        return 0   # replicas only: the render runs on one GPU
+    torch.cuda.set_device(local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    peaks = g.roofline(reps=2)
+    kind = args.rt_queue
+    ctxs = [g.RtTiles(kind, scene=sc, width=RT_SIZE, height=RT_SIZE, tile_px=RT_TILE, threads_per_tile=RT_TPT,
+                      max_bounces=RT_BOUNCES, queue_log2=RT_QLOG2, seed=RT_SEED) for sc in (0, 1)]
+    for _ in range(args.warmup):
+        for c in ctxs:
+            c.render()
+        flush.zero_()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    rays = [0, 0]
+    trace_ms = [0.0, 0.0]
+    dev_ms = 0.0
+    for _ in range(args.steps):
+        for sc, c in enumerate(ctxs):
+            r, _ = c.render()
+            rays[sc] += r["total_rays"]
+            trace_ms[sc] += r["trace_ms"]
+            dev_ms += r["total_ms"]
+            flush.zero_()          # between frames, outside the timed kernels
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    value = sum(rays) / (dev_ms * 1e3)
+    # end to end: the tile list in, the whole image out, wall clock
+    all_tiles = np.arange((RT_SIZE // RT_TILE) ** 2, dtype=np.int32)
+    e2e_s, e2e_rays, images = 0.0, 0, [None, None]
+    for _ in range(args.steps):
+        for sc, c in enumerate(ctxs):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r, images[sc] = c.render(all_tiles, image=True)
+            e2e_s += time.perf_counter() - t0
+            e2e_rays += r["total_rays"]
+    for c in ctxs:
+        c.close()
+    # parity of the last frames against the serial render (all host threads)
+    obuild.build()
+    cores = os.cpu_count() or 1
+    want_rays = []
+    for sc in (0, 1):
+        want = np.zeros((RT_SIZE, RT_SIZE, 3), np.float32)
+        want_rays.append(olib.lib().oracle_rt_bounce_render(sc, RT_SIZE, RT_SIZE, RT_BOUNCES, RT_SEED, cores,
+                                                            want.ctypes.data))
+        d = float(np.abs(images[sc] - want).max())
+        if d > 1e-4 or rays[sc] != want_rays[sc] * args.steps:
+            raise RuntimeError("scene %d differs from the serial render: max |diff| %g" % (sc, d))
+    # CPU baseline: the serial render, one core, on a 256x256 frame of each scene
+    t0 = time.perf_counter()
+    cpu_rays = 0
+    for sc in (0, 1):
+        tmp = np.zeros((256, 256, 3), np.float32)
+        cpu_rays += olib.lib().oracle_rt_bounce_render(sc, 256, 256, RT_BOUNCES, RT_SEED, 1, tmp.ctypes.data)
+    cpu_s = time.perf_counter() - t0
+    # roofline of the dominant kernel (scene 0's k_btrace)
+    flops0 = rays[0] * rt_flops_per_ray(*RT_SCENE_PRIMS[0])
+    achieved = flops0 / (trace_ms[0] * 1e-3) / 1e12
+    peak = peaks["fp32_gops"] / 1e3
+    line = {
+        "metric": RT_METRIC, "value": round(value, 2), "unit": "MRays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic scenes from a seed (512 random spheres; box room)",
+        "config": {"workload": "ray-bounce queues (%s), %dx%d, 1 spp, %d bounces, %dx%d-pixel tiles, %d threads "
+                               "and a 2^%d ring per tile, 32-byte rays; step = one frame of scene 0 and of scene 1"
+                               % (kind, RT_SIZE, RT_SIZE, RT_BOUNCES, RT_TILE, RT_TILE, RT_TPT, RT_QLOG2),
+                   "queue": kind, "rays_per_frame": {"scene0": want_rays[0], "scene1": want_rays[1]},
+                   "l2": "flushed between frames (256 MiB write)"},
+        "per_scene_ms": {"scene0": round(trace_ms[0] / args.steps, 3), "scene1": round(trace_ms[1] / args.steps, 3)},
+        "e2e": {"value": round(e2e_rays / (e2e_s * 1e6), 2), "unit": "MRays/s", "h2d_bytes_per_step": 2 * 4 * len(all_tiles),
+                "d2h_bytes_per_step": 2 * RT_SIZE * RT_SIZE * 12},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+        "roofline": {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3), "unit": "TFLOP/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_btrace<GCQ_GWFQ> (scene 0)",
+                     "flops_per_ray": rt_flops_per_ray(*RT_SCENE_PRIMS[0]),
+                     "peak_source": "unfused fp32 multiply+add rate measured in this run (gcq_roofline_measure)"},
+        "parity": "images within 1e-4 of the serial render (max |diff| 0 expected), ray counts equal",
+        "cpu_baseline": {"value": round(cpu_rays / cpu_s / 1e6, 3), "unit": "MRays/s", "cores": 1, "kind": "port",
+                         "sample": "oracle serial render (oracle/rt_cpu.cpp), 256x256 frame of each scene, 1 thread"},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def _serve_graphs(g, scales):
@@ -333,7 +452,8 @@ def _serve_graphs(g, scales):
 
 
 def run_served(args):
-    """Served BFS: one persistent kernel per step over the whole request set."""
+    """Served BFS and ray tiles: one persistent kernel per step over the whole
+    request set."""
     import numpy as np
     import gcq_gb300 as g
     from oracle import build as obuild, lib as olib
@@ -345,91 +465,152 @@ def run_served(args):
     t0 = time.perf_counter()
     graphs, names = _serve_graphs(g, scales)
     gen_s = time.perf_counter() - t0
+    ng = len(graphs)
     V = [len(o) - 1 for o, _ in graphs]
     E = [len(i) for _, i in graphs]
-    reqs = g.serve_requests(args.serve_requests, len(graphs), V, rate_per_s=args.serve_rate, seed=7)
+    n_bfs, n_tiles = args.serve_requests, args.serve_tiles
+    tiles_per_frame = (RT_SIZE // RT_TILE) ** 2
+    bfs = g.serve_requests(n_bfs, ng, V, rate_per_s=0, seed=7)
+    tiles = np.zeros(n_tiles, dtype=g.SERVE_REQ_DTYPE)
+    tiles["graph"] = ng + (np.arange(n_tiles) % 2)                  # both scenes
+    tiles["src"] = (np.arange(n_tiles) // 2) % tiles_per_frame
+    rng = np.random.default_rng(8)
+    reqs = np.concatenate([bfs, tiles])[rng.permutation(n_bfs + n_tiles)]
+    if args.serve_rate > 0:
+        reqs["arrival_ns"] = np.cumsum(rng.exponential(1e9 / args.serve_rate, size=len(reqs))).astype(np.uint64)
+    is_tile = reqs["graph"] >= ng
     peaks = g.roofline(reps=2)
-    srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0, threads=args.serve_threads)
+    srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0, threads=args.serve_threads,
+                   rt_scenes=2 if n_tiles else 0, rt_size=(RT_SIZE, RT_SIZE), rt_tile_px=RT_TILE,
+                   rt_max_bounces=RT_BOUNCES, rt_seed=RT_SEED)
     info = srv.info()
     for _ in range(args.warmup):
         srv.run(reqs)
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    kern_ms, wall_s, lat, items, stale, edges = 0.0, 0.0, [], 0, 0, 0
+    kern_ms, wall_s, lat, items, stale, edges, rays = 0.0, 0.0, [], 0, 0, 0, 0
     for _ in range(args.steps):
         t = time.perf_counter()
         res, st = srv.run(reqs)          # host requests in, host results out
         wall_s += time.perf_counter() - t
         kern_ms += st["kernel_ms"]
         lat.append((res["finish_ns"] - reqs["arrival_ns"]) / 1e6)
-        items += st["items"]; stale += st["stale"]; edges += st["edges"]
+        items += st["items"]; stale += st["stale"]; edges += st["edges"]; rays += st["rays"]
     clocks = sampler.stop()
-    # parity of the last step against the oracle on a sample of requests
+    # parity of the last step against the oracle: a sample of traversals, every tile
     obuild.build()
-    for i in range(0, len(reqs), max(1, len(reqs) // 16)):
+    bfs_idx = np.nonzero(~is_tile)[0]
+    for i in bfs_idx[:: max(1, len(bfs_idx) // 16)]:
         gi, src = int(reqs[i]["graph"]), int(reqs[i]["src"])
         want = olib.bfs_summary(graphs[gi][0], graphs[gi][1], src)
         got = (int(res[i]["checksum"]), int(res[i]["reached"]), int(res[i]["max_level"]))
         if got != want:
             raise RuntimeError("served traversal %d differs from the oracle: %s vs %s" % (i, got, want))
+    cores = os.cpu_count() or 1
+    if n_tiles:
+        for sc in (0, 1):
+            want = np.zeros((RT_SIZE, RT_SIZE, 3), np.float32)
+            olib.lib().oracle_rt_bounce_render(sc, RT_SIZE, RT_SIZE, RT_BOUNCES, RT_SEED, cores, want.ctypes.data)
+            sums = {}
+            for i in np.nonzero(reqs["graph"] == ng + sc)[0]:
+                tl = int(reqs[i]["src"])
+                if tl not in sums:
+                    sums[tl] = g.tile_checksum(want, tl, RT_TILE)
+                if int(res[i]["checksum"]) != sums[tl]:
+                    raise RuntimeError("served tile %d of scene %d differs from the serial render" % (tl, sc))
     srv.close()
-    n = len(reqs) * args.steps
-    value = n / (kern_ms * 1e-3)
-    e2e = n / wall_s
+    kern_s = kern_ms * 1e-3
     lat = np.concatenate(lat)
-    # one persistent BFS launch per request, timed on a sample of each graph's requests
+    lat_tile = lat.reshape(args.steps, -1)[:, is_tile].reshape(-1)
+    lat_bfs = lat.reshape(args.steps, -1)[:, ~is_tile].reshape(-1)
+    value = n_bfs * args.steps / kern_s
+    # one launch per request, timed on a sample of each target's requests
     per_graph_ms = {}
     for gi, (o, i) in enumerate(graphs):
-        srcs = reqs["src"][reqs["graph"] == gi][: args.serve_sample]
+        srcs = bfs["src"][bfs["graph"] == gi][: args.serve_sample]
         if len(srcs) == 0:
             continue
         with g.Bfs("gwfq", o, i, threads=8192) as b:
             b.run(int(srcs[0]), persistent=True, levels=False)
             ts = [b.run(int(sv), persistent=True, levels=False)[0]["total_ms"] for sv in srcs]
         per_graph_ms[gi] = float(np.mean(ts))
-    single_ms = sum(per_graph_ms[int(gg)] for gg in reqs["graph"])
-    single_rate = len(reqs) / (single_ms * 1e-3)
-    # serial BFS on the host (one core), one request per graph
+    per_scene_ms = {}
+    if n_tiles:
+        for sc in (0, 1):
+            with g.RtTiles("gwfq", scene=sc, width=RT_SIZE, height=RT_SIZE, tile_px=RT_TILE,
+                           threads_per_tile=RT_TPT, max_bounces=RT_BOUNCES, queue_log2=RT_QLOG2, seed=RT_SEED,
+                           max_tiles=1) as c:
+                c.render([0])
+                ts = []
+                for tl in range(0, tiles_per_frame, tiles_per_frame // 32):
+                    t = time.perf_counter()
+                    c.render([tl])
+                    ts.append((time.perf_counter() - t) * 1e3)
+            per_scene_ms[sc] = float(np.mean(ts))
+    single_bfs_ms = sum(per_graph_ms[int(gg)] for gg in bfs["graph"])
+    single_tile_ms = sum(per_scene_ms[int(gg) - ng] for gg in tiles["graph"])
+    single_rate = (n_bfs + n_tiles) / ((single_bfs_ms + single_tile_ms) * 1e-3)
+    served_rate = (n_bfs + n_tiles) * args.steps / kern_s
+    # serial BFS on the host (one core), one request per graph; serial tiles from a
+    # 256x256 frame of each scene
     cpu_ms = {}
     for gi, (o, i) in enumerate(graphs):
-        srcs = reqs["src"][reqs["graph"] == gi][:1]
+        srcs = bfs["src"][bfs["graph"] == gi][:1]
         if len(srcs):
             t = time.perf_counter()
             olib.bfs(o, i, int(srcs[0]))
             cpu_ms[gi] = (time.perf_counter() - t) * 1e3
-    cpu_total = sum(cpu_ms.get(int(gg), 0.0) for gg in reqs["graph"])
-    # HBM roofline: per traversal, offsets 4(V+1) + adjacency 4E + level probes 4E
-    # + level writes 4V + the sweep's read and reset 8V
-    alg_bytes = sum(4 * (V[gi] + 1) + 8 * E[gi] + 12 * V[gi] for gi in reqs["graph"].astype(int)) * args.steps
-    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    cpu_tile_ms = {}
+    for sc in (0, 1):
+        tmp = np.zeros((256, 256, 3), np.float32)
+        t = time.perf_counter()
+        olib.lib().oracle_rt_bounce_render(sc, 256, 256, RT_BOUNCES, RT_SEED, 1, tmp.ctypes.data)
+        cpu_tile_ms[sc] = (time.perf_counter() - t) * 1e3 * (RT_TILE * RT_TILE) / (256 * 256)
+    cpu_total = sum(cpu_ms.get(int(gg), 0.0) for gg in bfs["graph"]) + \
+        sum(cpu_tile_ms[int(gg) - ng] for gg in tiles["graph"])
+    # HBM roofline of the traversals: per traversal, offsets 4(V+1) + adjacency 4E +
+    # level probes 4E + level writes 4V + the sweep's read and reset 8V
+    alg_bytes = sum(4 * (V[gi] + 1) + 8 * E[gi] + 12 * V[gi] for gi in bfs["graph"].astype(int)) * args.steps
+    achieved = alg_bytes / kern_s / 1e9
+    pct = lambda a, q: round(float(np.percentile(a, q)), 3) if len(a) else None
     line = {
         "metric": SERVE_METRIC, "value": round(value, 2), "unit": "traversals/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(kern_ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-        "data": "synthetic graphs from seeds (R-MAT and grids), %d requests, %s arrivals"
-                % (len(reqs), "Poisson %.0f/s" % args.serve_rate if args.serve_rate else "closed-batch"),
-        "config": {"workload": "served BFS: %s; %d requests; 150 GiB level budget (%d slots, %.1f GB); "
-                               "%d persistent threads" % ("+".join(names), len(reqs), info["slots"],
-                                                          info["level_bytes"] / 1e9, info["threads"]),
+        "data": "synthetic graphs from seeds (R-MAT and grids) and the seeded benchmark scenes; %d traversal and "
+                "%d tile requests, %s arrivals" % (n_bfs, n_tiles, "Poisson %.0f/s" % args.serve_rate
+                                                   if args.serve_rate else "closed-batch"),
+        "config": {"workload": "served BFS + ray tiles: %s + scenes 0,1 (1024x1024, 32x32 tiles, 4 bounces); "
+                               "%d requests; 150 GiB budget (%d slots, %.1f GB of level arrays); %d persistent "
+                               "threads" % ("+".join(names), len(reqs), info["slots"], info["level_bytes"] / 1e9,
+                                            info["threads"]),
                    "graphs": {nm: {"V": v, "E": e} for nm, v, e in zip(names, V, E)},
                    "l2": "inputs larger than L2 (graphs %.1f GB)" % (sum(4 * (v + 1) + 4 * e for v, e in zip(V, E)) / 1e9)},
-        "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
-        "e2e": {"value": round(e2e, 2), "unit": "traversals/s", "h2d_bytes_per_step": len(reqs) * 16,
-                "d2h_bytes_per_step": len(reqs) * 40},
-        "one_launch_per_request": {"value": round(single_rate, 2), "unit": "traversals/s",
-                                   "speedup": round(value / single_rate, 2),
-                                   "sample": "%d persistent gcq_bfs_run launches per graph (G-WFQ, 8192 threads), "
-                                             "total_ms averaged and summed over the request mix" % args.serve_sample},
-        "work": {"items": items, "stale_items": stale, "edges_scanned": edges},
+        "tiles_per_s": round(n_tiles * args.steps / kern_s, 1),
+        "latency_ms": {"p50": pct(lat_bfs, 50), "p99": pct(lat_bfs, 99),
+                       "tiles_p50": pct(lat_tile, 50), "tiles_p99": pct(lat_tile, 99)},
+        "e2e": {"value": round(n_bfs * args.steps / wall_s, 2), "unit": "traversals/s",
+                "h2d_bytes_per_step": len(reqs) * 16, "d2h_bytes_per_step": len(reqs) * 40},
+        "one_launch_per_request": {
+            "value": round(single_rate, 2), "unit": "requests/s", "served_requests_per_s": round(served_rate, 2),
+            "speedup": round(served_rate / single_rate, 2),
+            "traversals_per_s": round(n_bfs / (single_bfs_ms * 1e-3), 2) if n_bfs else None,
+            "tiles_per_s": round(n_tiles / (single_tile_ms * 1e-3), 1) if n_tiles else None,
+            "sample": "%d persistent gcq_bfs_run launches per graph (G-WFQ, 8192 threads) and 32 single-tile "
+                      "gcq_rt_ctx_render calls per scene (wall clock), averaged and summed over the request mix"
+                      % args.serve_sample},
+        "work": {"items": items, "stale_items": stale, "edges_scanned": edges, "rays": rays},
         "gpu_launches": args.steps,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": round(peaks["hbm_gbs"], 1),
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
                      "kernel": "k_serve",
-                     "peak_source": "device copy bandwidth measured in this run (gcq_roofline_measure)"},
-        "cpu_baseline": {"value": round(len(reqs) / (cpu_total * 1e-3), 2), "unit": "traversals/s", "cores": 1,
-                         "kind": "port", "sample": "oracle serial BFS, one request per graph, summed over the mix"},
+                     "peak_source": "device copy bandwidth measured in this run (gcq_roofline_measure); achieved "
+                                    "counts the traversals' bytes only, over the whole mixed kernel time"},
+        "cpu_baseline": {"value": round(len(reqs) / (cpu_total * 1e-3), 2), "unit": "requests/s", "cores": 1,
+                         "kind": "port", "sample": "oracle serial BFS, one request per graph, and a 256x256 serial "
+                                                   "render per scene scaled to a tile, summed over the mix"},
         "graph_gen_s": round(gen_s, 1),
     }
     print(json.dumps(line), flush=True)
@@ -448,7 +629,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-queue", action="store_true", help="skip the table of all four queues")
-    ap.add_argument("--workload", choices=["tb", "served-bfs"], default="tb")
+    ap.add_argument("--workload", choices=["tb", "served-bfs", "rt"], default="tb")
+    ap.add_argument("--rt-queue", choices=["gwfq", "glfq", "sfq"], default="gwfq")
+    ap.add_argument("--serve-tiles", type=int, default=2048, help="ray-tile requests mixed into the served stream")
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--serve-rate", type=float, default=0.0, help="Poisson arrivals per second (0: closed batch)")
     ap.add_argument("--serve-scales", default="16,17,18,19,20,21,22")
@@ -461,6 +644,8 @@ def main():
         return run_reference(args)
     if args.workload == "served-bfs":
         return run_served(args)
+    if args.workload == "rt":
+        return run_rt(args)
     return run_gpu(args)
 
 

@@ -54,7 +54,7 @@ class FifoResult(C.Structure):
 class Roofline(C.Structure):
     _fields_ = [("r1_single", C.c_double), ("r1_warp", C.c_double), ("rs_lines", C.c_double),
                 ("rs_contig", C.c_double), ("rc_lines", C.c_double), ("rc128_lines", C.c_double),
-                ("hbm_gbs", C.c_double), ("sms", C.c_int), ("_pad", C.c_int)]
+                ("hbm_gbs", C.c_double), ("sms", C.c_int), ("_pad", C.c_int), ("fp32_gops", C.c_double)]
 
 
 class BfsResult(C.Structure):

@@ -72,6 +72,21 @@ __global__ void k_copy(const uint4* __restrict__ a, uint4* __restrict__ b, uint6
         b[i] = a[i];
 }
 
+// Unfused fp32 multiply and add (the ray tracer is built without contraction):
+// eight independent chains per thread, each step one rounded multiply and one
+// rounded add, so the count is 2 operations per step per chain.
+__global__ void k_fp32(float a, float b, uint32_t iters, float* sink) {
+    float x[8];
+    for (int k = 0; k < 8; ++k) x[k] = (float)(threadIdx.x + k);
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = __fadd_rn(__fmul_rn(x[k], a), b);
+    }
+    float s = 0.f;
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 1234.5f) *sink = s;   // keeps the chains live
+}
+
 struct timer {
     cudaEvent_t a, b;
     timer() { cudaEventCreate(&a); cudaEventCreate(&b); }
@@ -129,6 +144,9 @@ int gcq_roofline_measure(gcq_roofline* out, int reps) {
                          (double)threads * it_spread);
     out->rc128_lines = best([&] { k_spread_cas128<<<grid, block>>>(buf, lines, it_spread, sink); },
                             (double)threads * it_spread);
+    const uint32_t it_fp = 4096;
+    out->fp32_gops = best([&] { k_fp32<<<grid, block>>>(0.999f, 1e-3f, it_fp, (float*)sink); },
+                          (double)threads * it_fp * 16.0) / 1e9;
     GCQ_CUDA(cudaGetLastError());
     GCQ_CUDA(cudaFree(buf));
     // HBM: 2 GiB copy (well above L2)

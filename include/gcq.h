@@ -357,6 +357,7 @@ typedef struct gcq_roofline {
     double hbm_gbs;      /* device copy bandwidth */
     int sms;
     int _pad;
+    double fp32_gops;    /* unfused fp32 multiplies + adds per second (1e9), all SMs */
 } gcq_roofline;
 
 /* Run the microbenchmark (best of `reps`); synchronises the device. */
