@@ -159,11 +159,30 @@ __device__ __forceinline__ bool cas_upd_rel(u64a* p, uint64_t* expect, uint64_t 
     *expect = old;
     return ok;
 }
+__device__ __forceinline__ uint64_t cas_acq(u64a* p, uint64_t expect, uint64_t desired) {
+    uint64_t old;
+    asm volatile("atom.acquire.gpu.global.cas.b64 %0, [%1], %2, %3;"
+                 : "=l"(old) : "l"(p), "l"(expect), "l"(desired) : "memory");
+    return old;
+}
+// CAS with acq_rel (Release) or acquire ordering, refreshing `expect`.  A release
+// costs the issuing thread an extra L2 round trip on this GPU; acquire does not.
+template <bool Release>
+__device__ __forceinline__ bool cas_upd_ord(u64a* p, uint64_t* expect, uint64_t desired) {
+    const uint64_t old = Release ? cas(p, *expect, desired) : cas_acq(p, *expect, desired);
+    const bool ok = (old == *expect);
+    *expect = old;
+    return ok;
+}
 __device__ __forceinline__ bool cas_upd_rlx(u64a* p, uint64_t* expect, uint64_t desired) {
     const uint64_t old = cas_rlx(p, *expect, desired);
     const bool ok = (old == *expect);
     *expect = old;
     return ok;
+}
+// OR without a returned value: the issuing thread does not wait for it.
+__device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
+    asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ uint64_t fetch_or_acq(u64a* p, uint64_t v) {
     uint64_t old;

@@ -129,7 +129,10 @@ __device__ inline void catchup(ring* q, uint64_t tail, uint64_t head) {
 }
 
 // fq_enqueue, glf_queue.hpp:467-500.  Returns false only if the retry bound was
-// reached (error word set).
+// reached (error word set).  Publish: as gwf::try_enq (acq_rel entry CAS when the
+// caller wrote what the index refers to, acquire only when it ordered its accesses
+// itself).
+template <bool Publish = true>
 __device__ inline bool enqueue(ring* q, uint32_t index) {
     const cfg c = load_cfg(q);
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
@@ -139,7 +142,7 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
         // CAS first against the steady-state free slot (previous cycle, safe,
         // consumed); a mismatch returns the current value for the loop below.
         uint64_t E = ent::pack(tcyc - 1, true, BOT_C);
-        if (cas_upd_rel(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
+        if (cas_upd_ord<Publish>(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
             if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
             return true;
         }
@@ -150,7 +153,7 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
                 dekker_fence();
                 if (ld_rlx(&q->Head) > T) break;
             }
-            if (!cas_upd_rel(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
+            if (!cas_upd_ord<Publish>(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
                 if (spin >= GCQ_SPIN_LIMIT) break;
                 continue;
             }
@@ -170,26 +173,30 @@ __device__ inline uint32_t dequeue(ring* q) {
         const uint64_t H = warp_ticket(&q->Head, 1);
         const uint32_t hcyc = c.cycle_of(H);
         const uint32_t j = c.slot_of(H);
-        uint64_t E = ld_rlx(&c.entry[j]);
+        uint64_t E = ld_acq(&c.entry[j]);   // acquire: the payload reads follow a consume
         // bounded wait for the enqueuer holding this ticket (see gwf::try_deq)
         if (c.deq_wait && cycle_cmp(ent::cycle(E), hcyc) < 0 && ent::index(E) >= BOT) {
             uint32_t ns = 32;
             for (uint32_t w = 0; w < c.deq_wait; ++w) {
                 __nanosleep(ns);
                 ns = ns < 1024 ? ns * 2 : ns;
-                E = ld_rlx(&c.entry[j]);
+                E = ld_acq(&c.entry[j]);
                 if (!(cycle_cmp(ent::cycle(E), hcyc) < 0 && ent::index(E) >= BOT)) break;
             }
         }
-        for (;; ++spin) {
+        for (bool acquired = true;; ++spin) {
             const uint32_t ecyc = ent::cycle(E), eidx = ent::index(E);
             if (cycle_cmp(ecyc, hcyc) == 0 && eidx < BOT) {
-                fetch_or_acq(&c.entry[j], ent::CONSUME_MASK);   // acquire: payload reads follow
+                // E was read with acquire semantics (or is fenced now), so the OR that
+                // marks the slot consumed is issued without waiting for it
+                if (!acquired) fence_acq_rel();
+                red_or_rlx(&c.entry[j], ent::CONSUME_MASK);
                 return eidx;
             }
             if (cycle_cmp(ecyc, hcyc) >= 0 || spin >= GCQ_SPIN_LIMIT) break;
             const uint64_t nw = (eidx >= BOT) ? ent::pack(hcyc, ent::safe(E), BOT) : ent::pack(ecyc, false, eidx);
             if (cas_upd_rlx(&c.entry[j], &E, nw)) break;
+            acquired = false;
         }
         dekker_fence();
         const uint64_t T = ld_rlx(&q->Tail);
@@ -214,8 +221,8 @@ __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) {
 __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out) {
     const uint32_t idx = dequeue(&q->aq);
     if (idx == BOT) return false;
-    *out = ld_rlx(&q->data[idx]);
-    enqueue(&q->fq, idx);
+    *out = ld_acq(&q->data[idx]);   // orders the index's return to fq after the read
+    enqueue<false>(&q->fq, idx);
     return true;
 }
 

@@ -81,10 +81,14 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j
     }
 }
 
-// consume, gwf_ring.hpp:335-341
+// consume, gwf_ring.hpp:335-341.  The caller read `e` with acquire semantics (an
+// acquire load, or a relaxed access followed by an acq_rel fence), which orders
+// the payload reads after the enqueuer's release; the OR that marks the slot
+// consumed needs no ordering of its own, so it is issued without waiting for it
+// (an acquire RMW here costs a second L2 round trip on every dequeue).
 __device__ __forceinline__ void consume(const cfg& c, uint64_t h_raw, uint32_t j, uint64_t e, uint32_t tid) {
     if (!entry::enq(e)) finalize_request(c, h_raw, j, tid);
-    fetch_or_acq(&c.entry[j], entry::CONSUME_MASK);   // acquire: the payload reads follow
+    red_or_rlx(&c.entry[j], entry::CONSUME_MASK);
 }
 
 // catchup, gwf_ring.hpp:348-371
@@ -108,6 +112,12 @@ __device__ inline void catchup(ring* q, const cfg& c, uint64_t tail_raw, uint64_
 
 // ------------------------------------------------------------------ fast path
 // try_enq, gwf_ring.hpp:382-414.  0 on success, else the ticket tried.
+// Publish: the caller wrote what the index refers to before this call, and the
+// entry CAS is acq_rel -- release orders those writes before the index, acquire
+// orders the Threshold read after the CAS.  Without Publish the caller has ordered
+// its earlier accesses itself (with an acquire load), and the CAS is acquire only:
+// a release costs a further L2 round trip, an acquire nothing measurable.
+template <bool Publish = true>
 __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
     GCQ_STAT(c, stat::TRY_ENQ);
     const uint64_t T = c.counter(warp_ticket(&q->Tail, c.cinc()));
@@ -119,7 +129,7 @@ __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
     // the slot's current value, exactly what the load of gwf_ring.hpp:394 would
     // have read, so the code below continues from it.  Saves one L2 round trip.
     uint64_t E = entry::pack(0xFF, tcyc - 1, true, true, BOT_C);
-    if (cas_upd_rel(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
+    if (cas_upd_ord<Publish>(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
         if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
         return 0;
     }
@@ -132,7 +142,7 @@ __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
             if (c.counter(ld_rlx(&q->Head)) > T) return T;
         }
         const uint64_t nw = entry::pack(entry::note(E), tcyc, true, true, index);
-        if (!cas_upd_rel(&c.entry[j], &E, nw)) continue;   // release: publishes the payload
+        if (!cas_upd_ord<Publish>(&c.entry[j], &E, nw)) continue;
         if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
         return 0;
     }
@@ -147,7 +157,7 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
     const uint64_t H = c.counter(warp_ticket(&q->Head, c.cinc()));
     const uint32_t hcyc = c.cycle_of(H);
     const uint32_t j = c.slot_of(H);
-    uint64_t E = ld_rlx(&c.entry[j]);
+    uint64_t E = ld_acq(&c.entry[j]);   // acquire: see consume
     // The slot of an earlier cycle with no index: the enqueuer holding this ticket
     // may be about to fill it.  Marking it now would make that enqueuer retry with a
     // new ticket, and this dequeuer too; re-reading it a few times first (bounded,
@@ -157,7 +167,7 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
         for (uint32_t w = 0; w < c.deq_wait; ++w) {
             __nanosleep(ns);
             ns = ns < 1024 ? ns * 2 : ns;
-            E = ld_rlx(&c.entry[j]);
+            E = ld_acq(&c.entry[j]);
             if (!(cycle_cmp(entry::cycle(E), hcyc) < 0 && entry::empty_index(entry::index(E)))) {
                 GCQ_STAT(c, stat::DEQ_WAITED);
                 break;
@@ -169,6 +179,7 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
         const uint32_t ecyc = entry::cycle(E);
         const uint32_t eidx = entry::index(E);
         if (cycle_cmp(ecyc, hcyc) == 0 && !entry::empty_index(eidx)) {
+            if (spin) fence_acq_rel();   // E came from a relaxed CAS
             consume(c, H, j, E, tid);
             *out = eidx;
             return 0;
@@ -394,14 +405,15 @@ __device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid
 }
 
 // ------------------------------------------------------------------ top level
-// Enqueue_wf, gwf_ring.hpp:1234-1284
+// Enqueue_wf, gwf_ring.hpp:1234-1284 (Publish: see try_enq)
+template <bool Publish = true>
 __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
     const cfg c = load_cfg(q);
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return; }
     help_threads(q, c, tid);
     uint64_t tail = 0;
     for (uint32_t count = c.enq_patience; --count != 0;) {
-        tail = try_enq(q, c, index);
+        tail = try_enq<Publish>(q, c, index);
         if (tail == 0) return;
     }
     GCQ_STAT(c, stat::ENQ_SLOW);
@@ -488,11 +500,13 @@ __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t ti
     enqueue(&q->aq, idx, tid);   // its acq_rel CAS publishes data[idx]
     return true;
 }
+// The payload is read with an acquire load, which orders the index's return to fq
+// after it; the fq enqueue then needs no release of its own.
 __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid) {
     const uint32_t idx = dequeue(&q->aq, tid);
     if (idx == BOT) return false;
-    *out = ld_rlx(&q->data[idx]);
-    enqueue(&q->fq, idx, tid);   // releases the slot only after the read above
+    *out = ld_acq(&q->data[idx]);
+    enqueue<false>(&q->fq, idx, tid);
     return true;
 }
 // Enqueue for workloads whose consumers poll (the reference has none): fast-path
@@ -516,8 +530,8 @@ __device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t ti
 __device__ __forceinline__ bool try_dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->aq, tid, tries);
     if (idx == BOT) return false;
-    *out = ld_rlx(&q->data[idx]);
-    enqueue(&q->fq, idx, tid);
+    *out = ld_acq(&q->data[idx]);   // orders the index's return after the read
+    enqueue<false>(&q->fq, idx, tid);
     return true;
 }
 
