@@ -71,11 +71,15 @@ __device__ __forceinline__ V3 rand_in_unit_sphere(uint32_t& s) {
     return v3(0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ bool bhit_sphere(const BRay& r, const BSphere& sp, float tmax, BHit& h) {
-    const V3 oc = sub(r.o, sp.c);
-    const float a = dot3(r.d, r.d);
+// Closest hit in two passes: the loops find the nearest root (sphere centre and
+// radius as a float4, read through `cr`, which may be shared memory) and the
+// nearest quad, keeping only (t, index); the hit record is then built once for the
+// winner.  The roots, the comparisons and the record are the same float operations
+// as a loop that builds a record for every closer hit, so the result is too.
+__device__ __forceinline__ bool sphere_root(const BRay& r, float a, float4 s, float tmax, float* root_out) {
+    const V3 oc = sub(r.o, v3(s.x, s.y, s.z));
     const float half_b = dot3(oc, r.d);
-    const float c = dot3(oc, oc) - sp.r * sp.r;
+    const float c = dot3(oc, oc) - s.w * s.w;
     const float disc = half_b * half_b - a * c;
     if (disc < 0.f) return false;
     const float sq = sqrtf(disc);
@@ -84,18 +88,10 @@ __device__ __forceinline__ bool bhit_sphere(const BRay& r, const BSphere& sp, fl
         root = (-half_b + sq) / a;
         if (root <= 1e-3f || root >= tmax) return false;
     }
-    h.t = root;
-    h.p = add(r.o, scale(r.d, root));
-    const V3 outward = scale(sub(h.p, sp.c), 1.f / sp.r);
-    h.front = dot3(r.d, outward) < 0.f;
-    h.n = h.front ? outward : scale(outward, -1.f);
-    h.albedo = sp.albedo;
-    h.param = sp.param;
-    h.mat = sp.mat;
-    h.did_hit = true;
+    *root_out = root;
     return true;
 }
-__device__ __forceinline__ bool bhit_quad(const BRay& r, const BQuad& q, float tmax, BHit& h) {
+__device__ __forceinline__ bool quad_t(const BRay& r, const BQuad& q, float tmax, float* t_out) {
     const float da = comp(r.d, q.axis);
     if (fabsf(da) < 1e-8f) return false;
     const float t = (q.k - comp(r.o, q.axis)) / da;
@@ -104,30 +100,58 @@ __device__ __forceinline__ bool bhit_quad(const BRay& r, const BQuad& q, float t
     const float u = q.axis == 0 ? p.y : p.x;
     const float w = q.axis == 2 ? p.y : p.z;
     if (u < q.a0 || u > q.a1 || w < q.b0 || w > q.b1) return false;
-    h.t = t;
-    h.p = p;
-    const V3 outward = v3(q.axis == 0 ? 1.f : 0.f, q.axis == 1 ? 1.f : 0.f, q.axis == 2 ? 1.f : 0.f);
-    h.front = da < 0.f;
-    h.n = h.front ? outward : scale(outward, -1.f);
-    h.albedo = q.albedo;
-    h.param = 0.f;
-    h.mat = q.mat;
-    h.did_hit = true;
+    *t_out = t;
     return true;
 }
-__device__ __forceinline__ BHit btrace(const BRay& r, const BSphere* sph, int ns, const BQuad* quad, int nq) {
-    BHit best;
-    best.did_hit = false;
-    best.t = 1e30f;
+__device__ __forceinline__ float4 sphere_cr(const BSphere& sp) { return make_float4(sp.c.x, sp.c.y, sp.c.z, sp.r); }
+
+template <typename CR>
+__device__ __forceinline__ BHit btrace_with(const BRay& r, CR cr, const BSphere* sph, int ns, const BQuad* quad, int nq) {
+    const float a = dot3(r.d, r.d);
+    float best_t = 1e30f;
+    int best = -1;
+#pragma unroll 4
     for (int i = 0; i < ns; ++i) {
-        BHit h;
-        if (bhit_sphere(r, sph[i], best.t, h)) best = h;
+        float root;
+        if (sphere_root(r, a, cr(i), best_t, &root)) {
+            best_t = root;
+            best = i;
+        }
     }
+    int best_q = -1;
     for (int i = 0; i < nq; ++i) {
-        BHit h;
-        if (bhit_quad(r, quad[i], best.t, h)) best = h;
+        float t;
+        if (quad_t(r, quad[i], best_t, &t)) {
+            best_t = t;
+            best_q = i;
+        }
     }
-    return best;
+    BHit h;
+    h.t = best_t;
+    h.did_hit = (best_q >= 0 || best >= 0);
+    if (best_q >= 0) {
+        const BQuad& q = quad[best_q];
+        h.p = add(r.o, scale(r.d, best_t));
+        const V3 outward = v3(q.axis == 0 ? 1.f : 0.f, q.axis == 1 ? 1.f : 0.f, q.axis == 2 ? 1.f : 0.f);
+        h.front = comp(r.d, q.axis) < 0.f;
+        h.n = h.front ? outward : scale(outward, -1.f);
+        h.albedo = q.albedo;
+        h.param = 0.f;
+        h.mat = q.mat;
+    } else if (best >= 0) {
+        const BSphere& sp = sph[best];
+        h.p = add(r.o, scale(r.d, best_t));
+        const V3 outward = scale(sub(h.p, sp.c), 1.f / sp.r);
+        h.front = dot3(r.d, outward) < 0.f;
+        h.n = h.front ? outward : scale(outward, -1.f);
+        h.albedo = sp.albedo;
+        h.param = sp.param;
+        h.mat = sp.mat;
+    }
+    return h;
+}
+__device__ __forceinline__ BHit btrace(const BRay& r, const BSphere* sph, int ns, const BQuad* quad, int nq) {
+    return btrace_with(r, [sph](int i) { return sphere_cr(sph[i]); }, sph, ns, quad, nq);
 }
 
 // One bounce of a path: true with r and st updated when the path continues; false
