@@ -180,6 +180,19 @@ __device__ __forceinline__ bool cas_upd_rlx(u64a* p, uint64_t* expect, uint64_t 
     *expect = old;
     return ok;
 }
+// 128-bit exchange (atom.exch.b128, sm_90+) of the 16-byte-aligned pair at p;
+// the previous pair is returned in *olo, *ohi.
+template <bool Acquire>
+__device__ __forceinline__ void exch128(u64a* p, uint64_t lo, uint64_t hi, uint64_t* olo, uint64_t* ohi) {
+    if (Acquire)
+        asm volatile("{\n\t.reg .b128 val, old;\n\tmov.b128 val, {%2, %3};\n\t"
+                     "atom.acquire.gpu.global.exch.b128 old, [%4], val;\n\tmov.b128 {%0, %1}, old;\n\t}"
+                     : "=l"(*olo), "=l"(*ohi) : "l"(lo), "l"(hi), "l"(p) : "memory");
+    else
+        asm volatile("{\n\t.reg .b128 val, old;\n\tmov.b128 val, {%2, %3};\n\t"
+                     "atom.relaxed.gpu.global.exch.b128 old, [%4], val;\n\tmov.b128 {%0, %1}, old;\n\t}"
+                     : "=l"(*olo), "=l"(*ohi) : "l"(lo), "l"(hi), "l"(p) : "memory");
+}
 // OR without a returned value: the issuing thread does not wait for it.
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
