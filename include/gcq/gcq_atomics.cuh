@@ -193,6 +193,15 @@ __device__ __forceinline__ void exch128(u64a* p, uint64_t lo, uint64_t hi, uint6
                      "atom.relaxed.gpu.global.exch.b128 old, [%4], val;\n\tmov.b128 {%0, %1}, old;\n\t}"
                      : "=l"(*olo), "=l"(*ohi) : "l"(lo), "l"(hi), "l"(p) : "memory");
 }
+// A payload cell of an indirection queue (G-WFQ's MPMC): the value and a
+// full flag, written by the producer and read-and-emptied by the consumer as one
+// 128-bit atomic each.
+struct alignas(16) cell {
+    u64a value;
+    u64a full;   // CELL_FULL while it holds a payload, 0 once taken
+};
+constexpr uint64_t CELL_FULL = 1;
+
 // OR without a returned value: the issuing thread does not wait for it.
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -259,6 +268,31 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // pool) does not turn into one single-address atomic per operation.
 __device__ __forceinline__ void raise_error(u32a* err, unsigned int bits) {
     if (err && (ld_rlx(err) & bits) != bits) fetch_or(err, bits);
+}
+
+// Payload cells.  The reference writes data[idx], fences, then enqueues idx
+// (gwf_ring.hpp:1362-1370): a release, which costs the
+// producer a further L2 round trip on this GPU.  Here the producer writes
+// {value, full} with one 128-bit exchange it does not wait for and enqueues idx
+// with an acquire-only CAS; the consumer that dequeues idx takes the cell with a
+// 128-bit exchange to {0, 0}, retrying while the flag is clear -- the producer's
+// write was issued before the index was published, so it lands in bounded time
+// whatever the producer does next.  A taken cell is empty again before idx
+// returns to the free ring, so a full flag is always the current payload's.  The
+// free ring's acquire load orders the write after the previous take; the take's
+// acquire orders the index's return after it.
+__device__ __forceinline__ void put_cell(cell* c, uint64_t value) {
+    uint64_t olo, ohi;   // not waited for
+    exch128<false>(&c->value, value, CELL_FULL, &olo, &ohi);
+}
+__device__ __forceinline__ uint64_t take_cell(cell* c, u32a* err) {
+    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k) {
+        uint64_t v, f;
+        exch128<true>(&c->value, 0, 0, &v, &f);
+        if (f == CELL_FULL) return v;
+    }
+    raise_error(err, ERR_SPIN);
+    return 0;
 }
 
 // ---------------------------------------------------------------- tickets

