@@ -521,6 +521,13 @@ def run_served(args):
                     raise RuntimeError("served tile %d of scene %d differs from the serial render" % (tl, sc))
     srv.close()
     kern_s = kern_ms * 1e-3
+    # tile throughput over the span in which tiles were in the system (first tile
+    # arrival to last tile response), the kernel's other time being traversals
+    tiles_rate = None
+    if n_tiles:
+        t_first = float(reqs["arrival_ns"][is_tile].min())
+        t_last = float(res["finish_ns"][is_tile].max())
+        tiles_rate = n_tiles / max(1e-9, (t_last - t_first) * 1e-9)
     lat = np.concatenate(lat)
     lat_tile = lat.reshape(args.steps, -1)[:, is_tile].reshape(-1)
     lat_bfs = lat.reshape(args.steps, -1)[:, ~is_tile].reshape(-1)
@@ -588,6 +595,7 @@ def run_served(args):
                    "graphs": {nm: {"V": v, "E": e} for nm, v, e in zip(names, V, E)},
                    "l2": "inputs larger than L2 (graphs %.1f GB)" % (sum(4 * (v + 1) + 4 * e for v, e in zip(V, E)) / 1e9)},
         "tiles_per_s": round(n_tiles * args.steps / kern_s, 1),
+        "tiles_per_s_while_served": round(tiles_rate, 1) if tiles_rate else None,
         "latency_ms": {"p50": pct(lat_bfs, 50), "p99": pct(lat_bfs, 99),
                        "tiles_p50": pct(lat_tile, 50), "tiles_p99": pct(lat_tile, 99)},
         "e2e": {"value": round(n_bfs * args.steps / wall_s, 2), "unit": "traversals/s",
