@@ -91,14 +91,25 @@ template <int K> struct rtq;
 // ahead of Head).  Idle G-LFQ and SFQ tracer threads poll through it, so an empty
 // ring costs them two loads instead of Head tickets per poll (5x faster traces on
 // the 512-sphere scene with G-LFQ).  G-WFQ needs none: its dequeue returns on the
-// first load once the Threshold is negative, and timing showed the hint, with the
-// fast-path-only dequeue it calls for, no faster and less steady.
+// first load once the Threshold is negative, and timing showed the hint no faster
+// and less steady there.
+// G-WFQ tracer threads use the lock-free fast path on both sides: a thousand
+// pollers per ring keep the wait-free slow path from finishing promptly (its
+// tickets come one CAS at a time while pollers take Head tickets), and about one
+// render in ten of the 512-sphere scene took 33-36 ms instead of 3.4 once an
+// enqueue went slow.  With fast-path retries the trace is steady at 2.8 ms.
 template <> struct rtq<GCQ_GWFQ> {
     using R = gcq::gwf::ring;
     __device__ static bool maybe(const R*) { return true; }
-    __device__ static bool enq(R* q, uint32_t idx, uint32_t tid) { gcq::gwf::enqueue(q, idx, tid); return true; }
+    __device__ static bool enq(R* q, uint32_t idx, uint32_t) {
+        const gcq::gwf::cfg c = gcq::gwf::load_cfg(q);
+        for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k)
+            if (gcq::gwf::try_enq(q, c, idx) == 0) return true;   // release CAS publishes the ray
+        gcq::raise_error(c.err, gcq::ERR_SPIN);
+        return false;
+    }
     __device__ static bool deq(R* q, uint32_t* out, uint32_t tid) {
-        *out = gcq::gwf::dequeue(q, tid);
+        *out = gcq::gwf::try_dequeue(q, tid, 2);
         return *out != gcq::gwf::BOT;
     }
 };
