@@ -481,6 +481,7 @@ def run_served(args):
     is_tile = reqs["graph"] >= ng
     peaks = g.roofline(reps=2)
     srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0, threads=args.serve_threads,
+                   work_log2=args.serve_work_log2,
                    rt_scenes=2 if n_tiles else 0, rt_size=(RT_SIZE, RT_SIZE), rt_tile_px=RT_TILE,
                    rt_max_bounces=RT_BOUNCES, rt_seed=RT_SEED)
     info = srv.info()
@@ -590,8 +591,9 @@ def run_served(args):
                                                    if args.serve_rate else "closed-batch"),
         "config": {"workload": "served BFS + ray tiles: %s + scenes 0,1 (1024x1024, 32x32 tiles, 4 bounces); "
                                "%d requests; 150 GiB budget (%d slots, %.1f GB of level arrays); %d persistent "
-                               "threads" % ("+".join(names), len(reqs), info["slots"], info["level_bytes"] / 1e9,
-                                            info["threads"]),
+                               "threads; worklist 2^%s" % ("+".join(names), len(reqs), info["slots"],
+                                                           info["level_bytes"] / 1e9, info["threads"],
+                                                           args.serve_work_log2 or "auto"),
                    "graphs": {nm: {"V": v, "E": e} for nm, v, e in zip(names, V, E)},
                    "l2": "inputs larger than L2 (graphs %.1f GB)" % (sum(4 * (v + 1) + 4 * e for v, e in zip(V, E)) / 1e9)},
         "tiles_per_s": round(n_tiles * args.steps / kern_s, 1),
@@ -645,6 +647,8 @@ def main():
     ap.add_argument("--serve-scales", default="16,17,18,19,20,21,22")
     ap.add_argument("--serve-sample", type=int, default=3)
     ap.add_argument("--serve-threads", type=int, default=65536, help="persistent server threads (0: all resident)")
+    ap.add_argument("--serve-work-log2", type=int, default=29,
+                    help="worklist capacity log2 (0: the library default, 2^25 raised to 4x the largest graph)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -167,6 +167,9 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
     if (knobs) k = *knobs; else gcq_default_knobs(&k);
     if (max_threads == 0) return GCQ_EINVAL;
     if (kind != GCQ_WFQ && (capacity_log2 < 1 || capacity_log2 > 30)) return GCQ_EINVAL;
+    // the SCQ rings keep Threshold = 3N - 1 in an int (gwf_queue.hpp:313-323,
+    // glf_queue.hpp:127-138): N = 2^30 would overflow it
+    if ((kind == GCQ_GWFQ || kind == GCQ_GLFQ) && capacity_log2 > 29) return GCQ_EINVAL;
     // Identity slot mapping for both rings.  The reference's G-LFQ spreads
     // consecutive tickets over 128-B lines (glf_queue.hpp:116-120), against false
     // sharing between AMD wavefronts; with warp-aggregated tickets a warp's 32

@@ -749,7 +749,7 @@ int gcq_serve_create(int ngraphs, const int32_t* const* offsets, const int32_t* 
     // of the largest graph, so no graph waits for the worklist to drain completely
     uint32_t work_log2 = cfg->work_log2 ? cfg->work_log2 : 25;
     work_log2 = std::max({work_log2, log2_ceil((uint64_t)maxV) + 2, log2_ceil(threads)});
-    if (work_log2 > 30) return fail(GCQ_ECAPACITY);
+    if (work_log2 > 29) return fail(GCQ_ECAPACITY);   // the G-WFQ ring's limit
     s->work_cap = 1ull << work_log2;
     gcq_queue* q = nullptr;
     if ((rc = gcq_create(GCQ_GWFQ, work_log2, s->threads, &cfg->work_knobs, &q)) != GCQ_OK) return fail(rc);

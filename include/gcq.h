@@ -75,7 +75,8 @@ void gcq_default_knobs(gcq_knobs* k);
  * Envelope checks of the reference, made at run time:
  *   G-WFQ: max_threads <= 2^capacity_log2 (gwf_queue.hpp:320) and the cycle-bit
  *          inequality of gwf_queue.hpp:321-323;
- *   SFQ:   MAX_ID >= 2 * (max_threads + 1) (sfqueue_hip.hpp:45-47).
+ *   SFQ:   MAX_ID >= 2 * (max_threads + 1) (sfqueue_hip.hpp:45-47);
+ *   G-WFQ, G-LFQ: capacity_log2 <= 29 (their Threshold, 3N - 1, is an int).
  * For YMC capacity_log2 is ignored; the pool holds
  * max_threads * (3 * ymc_ops_per_thread + 128) cells plus 8 segments. */
 int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq_knobs* knobs,
@@ -384,7 +385,9 @@ typedef struct gcq_serve_cfg {
     uint64_t timeout_ns;    /* bound of every device wait; default 10 s */
     uint32_t max_slots;     /* level-array slots per graph, at most; default 1024 */
     uint32_t threads;       /* persistent threads; 0 = every resident thread */
-    uint32_t work_log2;     /* worklist capacity; default 25, raised to 4 x the largest graph */
+    uint32_t work_log2;     /* worklist capacity (<= 29); default 25, raised to 4 x the
+                               largest graph.  Each large traversal reserves V entries, so
+                               a larger worklist admits more of them at once */
     uint32_t _pad;
     uint64_t run_limit_ns;  /* a run gives up (GCQ_ETIMEDOUT) this long after the last
                                arrival; default 60 s */

@@ -146,3 +146,8 @@ def test_envelope_rejections(gcq):
     with pytest.raises(gcq.GcqError):
         gcq.Queue("sfq", 20, 8192)
     gcq.Queue("sfq", 20, 4095).close()
+    # the SCQ rings hold Threshold = 3N - 1 in an int: N <= 2^29
+    for kind in ("gwfq", "glfq"):
+        with pytest.raises(gcq.GcqError) as e:
+            gcq.Queue(kind, 30, 64)
+        assert e.value.status == gcq.EINVAL
