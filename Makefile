@@ -9,6 +9,7 @@
 #   make bfs QUEUE=glfq BFS_GRAPH=graphs/road_usa.mtx
 #   make rt QUEUE=gwfq SCENE=1 THREADS=1024 BOUNCES=4
 #   make rt-compact SCENE=2 BOUNCES=12      (the stream-compaction baseline)
+#   make rt-bench QUEUE=gwfq SCENE=0 THREADS=1024 BOUNCES=4   (benchmark scenes, 1024x1024)
 #
 # The linearizability checker is test infrastructure here (oracle/), run by the
 # test suite rather than by a make target.
@@ -89,7 +90,7 @@ BFS_BIN := $(BFS_BUILD_DIR)/bfs_$(QUEUE)
 HXX = $(CXX) -O2 -std=c++17 -Iinclude -I$(HARNESS) $(QUEUE_DEF)
 HLINK = -L$(LIB_DIR) -lgcq -Wl,-rpath,$(abspath $(LIB_DIR)) -pthread
 
-.PHONY: all lib rt rt-build rt-run rt-compact rt-compact-build rt-compact-run tb tb-build tb-run tb-build-fifo tb-run-fifo hist hist-build hist-run \
+.PHONY: all lib rt rt-build rt-run rt-bench rt-bench-build rt-bench-run rt-compact rt-compact-build rt-compact-run tb tb-build tb-run tb-build-fifo tb-run-fifo hist hist-build hist-run \
         hist-run-all bfs bfs-build bfs-build-all bfs-run bfs-sweep clean
 
 all: rt
@@ -108,6 +109,16 @@ rt-build: lib
 rt-run: rt-build
 	@echo "[RT] Running $(RT_BIN) scene=$(SCENE) bounces=$(BOUNCES) threads=$(THREADS)"
 	GPU_NAME="$(GPU_NAME)" $(RT_BIN) $(SCENE) $(BOUNCES) $(THREADS)
+
+rt-bench: rt-bench-run
+
+rt-bench-build: lib
+	@mkdir -p $(RT_BUILD_DIR)
+	@echo "[RT] Building $(RT_BUILD_DIR)/rt_bench_$(QUEUE) (benchmark scenes, qN=$(QUEUE_N))"
+	$(HXX) -DRT_QUEUE_N=$(QUEUE_N) $(EXTRA_FLAGS) $(HARNESS)/rt_bench.cpp -o $(RT_BUILD_DIR)/rt_bench_$(QUEUE) $(HLINK)
+
+rt-bench-run: rt-bench-build
+	GPU_NAME="$(GPU_NAME)" $(RT_BUILD_DIR)/rt_bench_$(QUEUE) $(SCENE) $(BOUNCES) $(THREADS)
 
 rt-compact: rt-compact-run
 

@@ -4,6 +4,8 @@ Outputs (git-ignored) under gcq_gb300/_build/:
   libgcq.so                 C ABI of include/gcq.h (queues, harnesses, BFS, RT, roofline)
   tb, history, bfs, rt      harness executables with the reference's argv and
                             Makefile knobs, linked against libgcq.so
+  rt_compact, rt_bench      the stream-compaction comparator and the
+                            benchmark-scene ray tracer, same form
 
 Every translation unit is compiled by nvcc for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a) in parallel, then linked with the

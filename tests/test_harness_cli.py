@@ -35,7 +35,7 @@ def _compile(name, out, defines):
 
 
 def test_harness_binaries_built(built):
-    for exe in ["tb", "history", "bfs", "rt", "rt_compact"]:
+    for exe in ["tb", "history", "bfs", "rt", "rt_compact", "rt_bench"]:
         assert os.access(os.path.join(built, exe), os.X_OK), exe
 
 
@@ -139,3 +139,21 @@ def test_rt_compact_cli(built, oracle_lib, tmp_path):
     got = np.frombuffer(data[len(b"P6\n1280 720\n255\n"):], np.uint8).reshape(720, 1280, 3)
     assert np.array_equal(got, np.clip(img * 255.0, 0, 255).astype(np.uint8))
     assert ",COMPACT,256,%d," % n in open(tmp_path / "rt_performance.csv").read()
+
+
+@pytest.mark.gpu
+def test_rt_bench_cli(built, oracle_lib, tmp_path):
+    """The benchmark-scene harness: the 1024x1024 room with G-LFQ; the PPM equals the
+    serial render quantised as the file is, and the ray count matches."""
+    r = _run([os.path.join(built, "rt_bench"), "1", "4", "1024"], cwd=tmp_path, env={"QUEUE": "glfq"})
+    assert r.returncode == 0, r.stderr
+    assert "Image saved: rtb_glfq_room.ppm" in r.stdout
+    img = np.zeros((1024, 1024, 3), np.float32)
+    n = oracle_lib.lib().oracle_rt_bounce_render(1, 1024, 1024, 4, 1, 16, img.ctypes.data)
+    assert "Total rays traced:  %d" % n in r.stdout
+    data = open(tmp_path / "rtb_glfq_room.ppm", "rb").read()
+    hdr = b"P6\n1024 1024\n255\n"
+    assert data.startswith(hdr) and len(data) == len(hdr) + 1024 * 1024 * 3
+    got = np.frombuffer(data[len(hdr):], np.uint8).reshape(1024, 1024, 3)
+    assert np.array_equal(got, np.clip(img * 255.0, 0, 255).astype(np.uint8))
+    assert "GLFQ,room,1024,4,1048576,%d," % n in open(tmp_path / "rt_bench_perf.csv").read()
