@@ -206,11 +206,6 @@ constexpr uint64_t CELL_FULL = 1;
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-__device__ __forceinline__ uint64_t fetch_or_acq(u64a* p, uint64_t v) {
-    uint64_t old;
-    asm volatile("atom.acquire.gpu.global.or.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
-    return old;
-}
 // CAS that reports success and refreshes `expect` with the observed value
 // (the C11 compare_exchange contract used by gwf_ring.hpp:93-99).
 __device__ __forceinline__ bool cas_upd(u64a* p, uint64_t* expect, uint64_t desired) {
