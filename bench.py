@@ -75,6 +75,21 @@ ATOMICS_PER_OP = 2.0 + 2.0 / 32.0
 METRIC = "queue succ Mops/s (G-WFQ balanced)"
 
 
+def whole_job(ms, count, device=None):
+    """Across the ranks of an initialised process group: the slowest rank's time and
+    the sum of all ranks' work (the whole-job value is sum / max).  With one rank,
+    or no process group, the inputs come back unchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms), float(count)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    c = torch.tensor([float(count)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return t.item(), c.item()
+
+
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -246,14 +261,7 @@ def run_gpu(args):
     if err & ~g.ERR_POOL:
         raise RuntimeError("queue error word 0x%x during the bench" % err)
     # whole-job: every rank's operations over the slowest rank's time
-    if world > 1:
-        t = torch.tensor([dev_ms, float(succ)], dtype=torch.float64, device=dev)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        dev_ms_all, succ_all = mx[0].item(), t[1].item()
-    else:
-        dev_ms_all, succ_all = dev_ms, float(succ)
+    dev_ms_all, succ_all = whole_job(dev_ms, succ, device=dev)
     value = succ_all / (dev_ms_all * 1e3)
 
     # ---- end to end through the C ABI with host buffers -----------------------
@@ -272,12 +280,7 @@ def run_gpu(args):
         cc = q.tb_chunk_host(0, threads, chunk, pay, block=BLOCK, stream=sptr)
         e2e_s += time.perf_counter() - t0
         e2e_ops += cc["enq_success"] + cc["deq_success"]
-    if world > 1:
-        t = torch.tensor([e2e_s, float(e2e_ops)], dtype=torch.float64, device=dev)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        e2e_s, e2e_ops = mx[0].item(), t[1].item()
+    e2e_s, e2e_ops = whole_job(e2e_s, e2e_ops, device=dev)
     e2e = e2e_ops / (e2e_s * 1e6)
 
     if rank == 0:
