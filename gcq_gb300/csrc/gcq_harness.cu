@@ -276,11 +276,24 @@ int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t thr
     if (rc != GCQ_OK) return rc;
     if (!host_payloads || !host_counters) return GCQ_EINVAL;
     cudaStream_t s = gcqi::as_stream(stream);
-    // device staging: payloads + counters, kept across calls of the same size
+    const size_t pbytes = (size_t)threads * chunk_ops * sizeof(uint32_t);
+    // Pinned host payloads are read by the kernel in place, over NVLink-C2C: each
+    // warp reads one 128-byte row per iteration, at the top of the iteration, so the
+    // transfer overlaps the queue operations instead of preceding them.  Pageable
+    // memory is staged through a device copy as before.
+    const uint32_t* direct = nullptr;
+    {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, host_payloads) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+            at.devicePointer)
+            direct = (const uint32_t*)at.devicePointer;
+        else
+            cudaGetLastError();
+    }
+    // device staging: payloads (pageable callers) + counters, kept across calls
     static thread_local void* stage = nullptr;
     static thread_local size_t stage_bytes = 0;
-    const size_t pbytes = (size_t)threads * chunk_ops * sizeof(uint32_t);
-    const size_t need = pbytes + 256;
+    const size_t need = (direct ? 0 : pbytes) + 256;
     if (stage_bytes < need) {
         if (stage) cudaFree(stage);
         stage = nullptr;
@@ -289,10 +302,11 @@ int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t thr
         stage_bytes = need;
     }
     uint32_t* d_pay = (uint32_t*)stage;
-    gcq_tb_counters* d_ctr = (gcq_tb_counters*)((char*)stage + ((pbytes + 127) / 128) * 128);
-    GCQ_CUDA(cudaMemcpyAsync(d_pay, host_payloads, pbytes, cudaMemcpyHostToDevice, s));
+    gcq_tb_counters* d_ctr =
+        (gcq_tb_counters*)((char*)stage + (direct ? 0 : ((pbytes + 127) / 128) * 128));
+    if (!direct) GCQ_CUDA(cudaMemcpyAsync(d_pay, host_payloads, pbytes, cudaMemcpyHostToDevice, s));
     GCQ_CUDA(cudaMemsetAsync(d_ctr, 0, sizeof(gcq_tb_counters), s));
-    rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, d_pay, d_ctr, s);
+    rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, direct ? direct : d_pay, d_ctr, s);
     if (rc != GCQ_OK) return rc;
     GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
     GCQ_CUDA(cudaStreamSynchronize(s));

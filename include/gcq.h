@@ -153,10 +153,11 @@ typedef struct gcq_tb_counters {
 int gcq_tb_launch(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
                   uint32_t chunk_ops, uint64_t seed, void* dev_counters, void* stream);
 
-/* End-to-end chunk through host memory: copies threads*chunk_ops uint32 payloads
- * (payload i of thread t at host_payloads[i * threads + t]) to the device, runs
- * one chunk with them, and copies the counters of that chunk back to host_counters.
- * host_payloads should be pinned for full copy bandwidth. */
+/* End-to-end chunk through host memory: moves threads*chunk_ops uint32 payloads
+ * (payload i of thread t at host_payloads[i * threads + t]) to the GPU, runs one
+ * chunk with them, and copies the counters of that chunk back to host_counters.
+ * Pinned payloads (cudaHostAlloc / cudaHostRegister) are read by the kernel in
+ * place over the host link while it runs; pageable ones are copied first. */
 int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
                       uint32_t chunk_ops, const uint32_t* host_payloads, gcq_tb_counters* host_counters,
                       void* stream);

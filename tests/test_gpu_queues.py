@@ -137,6 +137,27 @@ def test_chunk_host_matches_device_counts(gcq):
         assert c["deq_success"] >= c["enq_success"] - threads
 
 
+def test_tb_chunk_host_pinned_in_place(gcq):
+    """Pinned payloads are read by the kernel in place over the host link; the
+    counts equal those of the staged (pageable) path for the same payloads."""
+    torch = pytest.importorskip("torch")
+    threads, chunk = 8192, 16
+    rng = np.random.default_rng(6)
+    vals = rng.integers(0, 2**32, size=threads * chunk, dtype=np.uint64).astype(np.uint32)
+    pinned = torch.empty(threads * chunk, dtype=torch.int32).pin_memory()
+    pin = pinned.numpy().view(np.uint32)
+    pin[:] = vals
+    for mode in (0, 1):
+        with gcq.Queue("gwfq", 15, threads) as q:
+            a = q.tb_chunk_host(mode, threads, chunk, pin)
+        with gcq.Queue("gwfq", 15, threads) as q:
+            b = q.tb_chunk_host(mode, threads, chunk, vals.copy())
+        assert a["enq_success"] + a["enq_fail"] == b["enq_success"] + b["enq_fail"]
+        if mode == 0:
+            assert a["enq_success"] == b["enq_success"] == threads * chunk
+            assert a["deq_success"] + a["deq_empty"] == threads * chunk
+
+
 def test_envelope_rejections(gcq):
     # G-WFQ requires max_threads <= capacity (gwf_queue.hpp:320)
     with pytest.raises(gcq.GcqError) as e:
