@@ -567,10 +567,14 @@ def run_served(args):
         reqs["arrival_ns"] = np.cumsum(rng.exponential(1e9 / args.serve_rate, size=len(reqs))).astype(np.uint64)
     is_tile = reqs["graph"] >= ng
     peaks = g.roofline(reps=2)
-    srv = g.Server(graphs, budget_bytes=150 << 30, run_limit_s=60.0, threads=args.serve_threads,
-                   work_log2=args.serve_work_log2,
-                   rt_scenes=2 if n_tiles else 0, rt_size=(RT_SIZE, RT_SIZE), rt_tile_px=RT_TILE,
-                   rt_max_bounces=RT_BOUNCES, rt_seed=RT_SEED)
+    common = dict(budget_bytes=150 << 30, run_limit_s=60.0, rt_scenes=2 if n_tiles else 0,
+                  rt_size=(RT_SIZE, RT_SIZE), rt_tile_px=RT_TILE, rt_max_bounces=RT_BOUNCES, rt_seed=RT_SEED)
+    tuned, tune_table = dict(threads=args.serve_threads, work_log2=args.serve_work_log2), None
+    if args.serve_autotune:
+        sample = reqs[: min(len(reqs), 384)].copy()
+        sample["arrival_ns"] = 0
+        tuned, tune_table = g.serve_autotune(graphs, sample, **common)
+    srv = g.Server(graphs, **common, **tuned)
     info = srv.info()
     for _ in range(args.warmup):
         srv.run(reqs)
@@ -586,6 +590,22 @@ def run_served(args):
         lat.append((res["finish_ns"] - reqs["arrival_ns"]) / 1e6)
         items += st["items"]; stale += st["stale"]; edges += st["edges"]; rays += st["rays"]
     clocks = sampler.stop()
+    # an open-loop Poisson stream of the same requests at 70 % of the closed-batch
+    # rate, for latency under a load the server keeps up with
+    poisson = None
+    if args.serve_poisson:
+        rate = 0.7 * len(reqs) * args.steps / (kern_ms * 1e-3)
+        preqs = reqs.copy()
+        prng = np.random.default_rng(9)
+        preqs["arrival_ns"] = np.cumsum(prng.exponential(1e9 / rate, size=len(preqs))).astype(np.uint64)
+        pres, pst = srv.run(preqs)
+        plat = (pres["finish_ns"] - preqs["arrival_ns"]) / 1e6
+        span = float(pres["finish_ns"].max()) * 1e-9
+        poisson = {"offered_requests_per_s": round(rate, 1), "served_requests_per_s": round(len(preqs) / span, 1),
+                   "p50_ms": round(float(np.percentile(plat[~is_tile], 50)), 3),
+                   "p99_ms": round(float(np.percentile(plat[~is_tile], 99)), 3),
+                   "tiles_p50_ms": round(float(np.percentile(plat[is_tile], 50)), 3) if n_tiles else None,
+                   "tiles_p99_ms": round(float(np.percentile(plat[is_tile], 99)), 3) if n_tiles else None}
     # parity of the last step against the oracle: a sample of traversals, every tile
     obuild.build()
     bfs_idx = np.nonzero(~is_tile)[0]
@@ -684,13 +704,16 @@ def run_served(args):
                                "%d requests; 150 GiB budget (%d slots, %.1f GB of level arrays); %d persistent "
                                "threads; worklist 2^%s" % ("+".join(names), len(reqs), info["slots"],
                                                            info["level_bytes"] / 1e9, info["threads"],
-                                                           args.serve_work_log2 or "auto"),
+                                                           tuned.get("work_log2") or "auto"),
                    "graphs": {nm: {"V": v, "E": e} for nm, v, e in zip(names, V, E)},
                    "l2": "inputs larger than L2 (graphs %.1f GB)" % (sum(4 * (v + 1) + 4 * e for v, e in zip(V, E)) / 1e9)},
         "tiles_per_s": round(n_tiles * args.steps / kern_s, 1),
         "tiles_per_s_while_served": round(tiles_rate, 1) if tiles_rate else None,
         "latency_ms": {"p50": pct(lat_bfs, 50), "p99": pct(lat_bfs, 99),
                        "tiles_p50": pct(lat_tile, 50), "tiles_p99": pct(lat_tile, 99)},
+        "poisson": poisson,
+        "autotune": {"chosen": tuned, "candidates": [{"config": c, "requests_per_s": None if r is None else round(r, 1)}
+                                                    for c, r in tune_table]} if tune_table else None,
         "e2e": {"value": round(n_bfs * args.steps / wall_s, 2), "unit": "traversals/s",
                 "h2d_bytes_per_step": len(reqs) * 16, "d2h_bytes_per_step": len(reqs) * 40},
         "one_launch_per_request": {
@@ -743,6 +766,10 @@ def main():
     ap.add_argument("--serve-threads", type=int, default=65536, help="persistent server threads (0: all resident)")
     ap.add_argument("--serve-work-log2", type=int, default=29,
                     help="worklist capacity log2 (0: the library default, 2^25 raised to 4x the largest graph)")
+    ap.add_argument("--no-serve-autotune", dest="serve_autotune", action="store_false",
+                    help="use --serve-threads / --serve-work-log2 instead of timing candidates on a sample")
+    ap.add_argument("--no-serve-poisson", dest="serve_poisson", action="store_false",
+                    help="skip the open-loop Poisson run at 70 %% of the closed-batch rate")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -497,6 +497,30 @@ class Server:
             pass
 
 
+def serve_autotune(graphs, sample_reqs: np.ndarray, candidates=None, **server_kw):
+    """Pick the served engine's persistent-thread count and worklist size by timing
+    a sample of requests on each candidate (the reference has no server; its BFS
+    harness takes the thread count from the command line).  Returns (best keyword
+    arguments for Server, [(candidate, requests per second or None)])."""
+    if candidates is None:
+        candidates = [dict(threads=t, work_log2=w) for t in (32768, 65536, 0) for w in (28, 29)]
+    table = []
+    for cand in candidates:
+        kw = dict(server_kw)
+        kw.update(cand)
+        try:
+            with Server(graphs, **kw) as srv:
+                srv.run(sample_reqs)
+                _, st = srv.run(sample_reqs)
+            table.append((cand, len(sample_reqs) / (st["kernel_ms"] * 1e-3)))
+        except GcqError:
+            table.append((cand, None))
+    ok = [t for t in table if t[1]]
+    if not ok:
+        raise GcqError(EINVAL, "serve_autotune: no candidate ran")
+    return max(ok, key=lambda t: t[1])[0], table
+
+
 def serve_requests(n: int, ngraphs: int, V, rate_per_s: float = 0.0, seed: int = 1, weights=None):
     """A seeded request schedule: graph drawn by `weights` (uniform by default), a
     uniform source vertex, Poisson arrivals at `rate_per_s` (0: all at time 0)."""
