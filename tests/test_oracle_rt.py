@@ -70,3 +70,4 @@ def test_tile_checksum_formula():
         assert gcq.tile_checksum(img, tile, 32) == want
     xs = np.array([0, 1, 2 ** 63, 2 ** 64 - 1], dtype=np.uint64)
     assert [int(v) for v in gcq.splitmix64(xs)] == [_splitmix_py(int(v)) for v in xs]
+
