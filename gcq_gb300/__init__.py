@@ -612,6 +612,12 @@ class RtTiles:
     def __exit__(self, *exc):
         self.close()
 
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def rt_compact_render(scene: int = 0, width: int = 1280, height: int = 720, max_bounces: int = 4):
     """Render one frame with the stream-compaction baseline; returns (result, image HxWx3)."""
