@@ -54,3 +54,34 @@ def test_library_loads_without_gpu(built_lib):
     assert k.ymc_patience == 16 and k.ymc_ops_per_thread == 512
 
 
+
+
+def test_argument_checks_without_gpu(built_lib):
+    """Argument checks that return before any CUDA call: invalid configurations are
+    rejected with their status on a machine without a GPU."""
+    import ctypes
+    import gcq_gb300 as g
+    L = g.lib()
+    q = ctypes.c_void_p()
+    # SCQ rings: Threshold = 3N - 1 is an int, so N <= 2^29
+    assert L.gcq_create(g.KINDS["gwfq"], 30, 64, None, ctypes.byref(q)) == g.EINVAL
+    assert L.gcq_create(g.KINDS["glfq"], 30, 64, None, ctypes.byref(q)) == g.EINVAL
+    assert L.gcq_create(g.KINDS["gwfq"], 15, 0, None, ctypes.byref(q)) == g.EINVAL
+    r = g.RtResult()
+    img = None
+    # benchmark-scene renderer: scene, size, queue kind, ring too small for a tile
+    cases = [((g.KINDS["gwfq"], 2, 64, 64, 32, 64, 4, 15, 1), g.EINVAL),
+             ((g.KINDS["gwfq"], 0, 0, 64, 32, 64, 4, 15, 1), g.EINVAL),
+             ((g.KINDS["gwfq"], 0, 64, 64, 32, 64, -1, 15, 1), g.EINVAL),
+             ((g.KINDS["wfq"], 0, 64, 64, 32, 64, 4, 15, 1), g.EUNSUPPORTED),
+             ((g.KINDS["gwfq"], 0, 64, 64, 32, 64, 4, 9, 1), g.ECAPACITY)]
+    for args, want in cases:
+        assert L.gcq_rt_bounce_render(*args, img, ctypes.byref(r)) == want, args
+    ctx = ctypes.c_void_p()
+    assert L.gcq_rt_ctx_create(g.KINDS["sfq"], 1, 64, 64, 64, 32, 4, 10, 1, 0, ctypes.byref(ctx)) == g.ECAPACITY
+    assert L.gcq_rt_ctx_render(None, None, 0, None, ctypes.byref(r)) == g.EINVAL
+    # served engine defaults
+    cfg = g.ServeCfg()
+    L.gcq_serve_default_cfg(ctypes.byref(cfg))
+    assert cfg.budget_bytes == 150 << 30 and cfg.rt_scenes == 0
+    assert (cfg.rt_width, cfg.rt_height, cfg.rt_tile_px, cfg.rt_max_bounces, cfg.rt_slots) == (1024, 1024, 32, 4, 1024)
