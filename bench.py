@@ -41,7 +41,9 @@ queue threads, 3 warm-up and 10 timed traversals each; depths are checked agains
 the oracle's serial BFS.  Metric: graph A traversals per second (asynchronous, 8192
 threads).
 
---impl reference runs the reference algorithm on the host cores instead: the
+--impl reference runs the reference algorithm on the host cores instead; with
+--workload rt it is the oracle's serial render on every host core, with --workload
+bfs the oracle's serial BFS of graph A: the
 reference is HIP for AMD GPUs and cannot run here, so its arm is the oracle's CPU
 restatement of the same G-WFQ (oracle/cpu_queues.cpp), on every host core.
 
@@ -175,12 +177,65 @@ def per_queue(g):
     return out
 
 
+def _reference_line(args, metric, value, unit, config, sample, cores, dtype, steps, extra=None):
+    line = {"impl": "reference", "metric": metric, "value": round(value, 3), "unit": unit,
+            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config,
+            "cpu_baseline": {"value": round(value, 3), "unit": unit, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra or {})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_rt(args, olib, cores):
+    """The serial render of the benchmark scenes on every host core (the reference's
+    RT harness has no CPU path; its algorithm for these scenes is the oracle's)."""
+    import numpy as np
+    steps = max(1, min(args.steps, 3))
+    img = np.zeros((RT_SIZE, RT_SIZE, 3), np.float32)
+    olib.lib().oracle_rt_bounce_render(1, 256, 256, RT_BOUNCES, RT_SEED, cores, img.ctypes.data)   # warm-up
+    rays, t0 = 0, time.perf_counter()
+    for _ in range(steps):
+        for sc in (0, 1):
+            rays += olib.lib().oracle_rt_bounce_render(sc, RT_SIZE, RT_SIZE, RT_BOUNCES, RT_SEED, cores,
+                                                       img.ctypes.data)
+    sec = time.perf_counter() - t0
+    return _reference_line(args, RT_METRIC, rays / sec / 1e6, "MRays/s",
+                           {"workload": "serial render (oracle/rt_cpu.cpp) of both benchmark scenes, %dx%d, "
+                                        "1 spp, %d bounces, rows split over %d host threads" % (RT_SIZE, RT_SIZE,
+                                                                                             RT_BOUNCES, cores)},
+                           "%d frame(s) of each scene, %d threads" % (steps, cores), cores, "f32", steps,
+                           {"ms_per_step": round(sec * 1e3 / steps, 3)})
+
+
+def run_reference_bfs(args, olib, cores):
+    """The serial BFS of graph A from vertex 0 (one core)."""
+    import gcq_gb300 as g   # host-side graph generator only
+    off, idx = g.graph_grid(4096, 4096, 0.6, 0.01, 2)
+    steps = max(1, min(args.steps, 3))
+    olib.bfs(off, idx, 0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        olib.bfs(off, idx, 0)
+    sec = (time.perf_counter() - t0) / steps
+    return _reference_line(args, BFS_METRIC, 1.0 / sec, "traversals/s",
+                           {"workload": "serial BFS (oracle/bfs_serial.cpp) of graph A from vertex 0"},
+                           "%d traversal(s) of graph A, 1 thread" % steps, 1, "int32", steps,
+                           {"ms_per_step": round(sec * 1e3, 3)})
+
+
 def run_reference(args):
     rank, world, _ = _env_rank()
     if rank != 0:
         return 0
     from oracle import build as obuild, lib as olib
     obuild.build()
+    if args.workload == "rt":
+        return run_reference_rt(args, olib, os.cpu_count() or 1)
+    if args.workload == "bfs":
+        return run_reference_bfs(args, olib, os.cpu_count() or 1)
     cores = os.cpu_count() or 1
     step_ms = 400.0
     for _ in range(args.warmup):
