@@ -41,11 +41,11 @@ queue threads, 3 warm-up and 10 timed traversals each; depths are checked agains
 the oracle's serial BFS.  Metric: graph A traversals per second (asynchronous, 8192
 threads).
 
---impl reference runs the reference algorithm on the host cores instead; with
---workload rt it is the oracle's serial render on every host core, with --workload
-bfs the oracle's serial BFS of graph A: the
+--impl reference runs the reference algorithm on the host cores instead: the
 reference is HIP for AMD GPUs and cannot run here, so its arm is the oracle's CPU
-restatement of the same G-WFQ (oracle/cpu_queues.cpp), on every host core.
+restatement of the same G-WFQ (oracle/cpu_queues.cpp), on every host core; with
+--workload rt it is the oracle's serial render on every host core, with --workload
+bfs the oracle's serial BFS of graph A.
 
 Multi-GPU (torchrun, --gpus N): replicas only -- a queue is one linearizable object
 with global counters, so each rank runs its own queue; value = all ranks' operations
