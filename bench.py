@@ -45,7 +45,8 @@ threads).
 reference is HIP for AMD GPUs and cannot run here, so its arm is the oracle's CPU
 restatement of the same G-WFQ (oracle/cpu_queues.cpp), on every host core; with
 --workload rt it is the oracle's serial render on every host core, with --workload
-bfs the oracle's serial BFS of graph A.
+bfs the oracle's serial BFS of graph A, with --workload served-bfs the mix's
+requests one at a time on one core (sampled per graph and scene).
 
 Multi-GPU (torchrun, --gpus N): replicas only -- a queue is one linearizable object
 with global counters, so each rank runs its own queue; value = all ranks' operations
@@ -226,6 +227,41 @@ def run_reference_bfs(args, olib, cores):
                            {"ms_per_step": round(sec * 1e3, 3)})
 
 
+def run_reference_served(args, olib, cores):
+    """The served mix's requests run one at a time on the host: the oracle's serial
+    BFS from one source per graph and a 256x256 serial render per scene scaled to a
+    tile, summed over the same request mix as the GPU arm."""
+    import numpy as np
+    import gcq_gb300 as g   # host-side graph generators only
+    scales = [int(x) for x in args.serve_scales.split(",") if x]
+    graphs, names = _serve_graphs(g, scales)
+    ng = len(graphs)
+    V = [len(o) - 1 for o, _ in graphs]
+    bfs = g.serve_requests(args.serve_requests, ng, V, rate_per_s=0, seed=7)
+    per_graph = {}
+    for gi, (o, i) in enumerate(graphs):
+        srcs = bfs["src"][bfs["graph"] == gi][:1]
+        if len(srcs):
+            t0 = time.perf_counter()
+            olib.bfs(o, i, int(srcs[0]))
+            per_graph[gi] = time.perf_counter() - t0
+    per_tile = {}
+    for sc in (0, 1):
+        tmp = np.zeros((256, 256, 3), np.float32)
+        t0 = time.perf_counter()
+        olib.lib().oracle_rt_bounce_render(sc, 256, 256, RT_BOUNCES, RT_SEED, 1, tmp.ctypes.data)
+        per_tile[sc] = (time.perf_counter() - t0) * (RT_TILE * RT_TILE) / (256 * 256)
+    n_tiles = args.serve_tiles
+    total = sum(per_graph[int(gg)] for gg in bfs["graph"]) + sum(per_tile[k % 2] for k in range(n_tiles))
+    rate = (args.serve_requests + n_tiles) / total
+    return _reference_line(args, SERVE_METRIC, args.serve_requests / total, "traversals/s",
+                           {"workload": "the served mix (%s + %d tiles) one request at a time on one host core"
+                                        % ("+".join(names), n_tiles)},
+                           "oracle serial BFS, one request per graph, and a 256x256 serial render per scene "
+                           "scaled to a tile, summed over the mix", 1, "int32", 1,
+                           {"requests_per_s": round(rate, 3)})
+
+
 def run_reference(args):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -236,6 +272,8 @@ def run_reference(args):
         return run_reference_rt(args, olib, os.cpu_count() or 1)
     if args.workload == "bfs":
         return run_reference_bfs(args, olib, os.cpu_count() or 1)
+    if args.workload == "served-bfs":
+        return run_reference_served(args, olib, os.cpu_count() or 1)
     cores = os.cpu_count() or 1
     step_ms = 400.0
     for _ in range(args.warmup):

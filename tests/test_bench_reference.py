@@ -13,6 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 @pytest.mark.parametrize("workload, metric_start, unit", [
     ("rt", "RT MRays/s", "MRays/s"),
     ("bfs", "BFS traversals/s", "traversals/s"),
+    ("served-bfs", "served BFS traversals/s", "traversals/s"),
 ])
 def test_reference_arm_line(workload, metric_start, unit):
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", workload, "--steps", "1"],
