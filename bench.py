@@ -9,7 +9,8 @@ chunk launch over all threads.  Metric: successful queue operations per second
   value    device time of K chunk launches (CUDA events on the launching stream),
            L2 flushed between steps by writing a 256 MiB buffer
   e2e      the same chunks through the C-ABI entry point gcq_tb_chunk_host with the
-           payloads in pinned host memory: host->device copy, kernel, and the
+           payloads in pinned host memory: their transfer to the device (the kernel
+           reads pinned payloads in place over the host link), the kernel, and the
            counters read back to the host are inside the timed region
   roofline the chunk kernel against the measured L2 atomic throughput of this GPU
            (gcq_roofline_measure, run in the same process)
