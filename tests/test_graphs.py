@@ -118,3 +118,23 @@ def test_load_rejects(gcq_host, tmp_path):
         gcq_host.graph_load(str(bad))
     with pytest.raises(gcq_gb300.GcqError):
         gcq_host.graph_load(str(tmp_path / "missing.mtx"))
+
+
+@pytest.mark.parametrize("which", ["grid", "rmat"])
+def test_oracle_bfs_against_scipy(gcq_host, oracle_lib, which):
+    """The serial BFS that pins every GPU traversal, against an independent
+    implementation (scipy's unweighted shortest paths) on generated graphs."""
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    if which == "grid":
+        off, idx = gcq_host.graph_grid(60, 70, 0.6, 0.01, 3)
+    else:
+        off, idx = gcq_host.graph_rmat(11, 8, 0.57, 0.19, 0.19, seed=4)
+    V = len(off) - 1
+    A = sp.csr_matrix((np.ones(len(idx)), idx, off), shape=(V, V))
+    for src in (0, V // 3, V - 1):
+        want = csgraph.shortest_path(A, method="D", unweighted=True, indices=src)
+        want = np.where(np.isinf(want), -1, want).astype(np.int32)
+        got, ecc = oracle_lib.bfs(off, idx, src)
+        assert np.array_equal(got, want), (which, src)
+        assert ecc == want.max()
