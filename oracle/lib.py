@@ -2,7 +2,8 @@
 
 Covers the FIFO linearizability checker (lincheck.cpp), the std::atomic CPU
 restatements of the four queues (cpu_queues.cpp), the serial BFS
-(bfs_serial.cpp) and the serial ray tracer (rt_cpu.cpp).
+(bfs_serial.cpp) and the serial renders (rt_cpu.cpp: the reference's scenes, the
+stream-compaction comparator's shading, and the benchmark scenes).
 """
 from __future__ import annotations
 
