@@ -7,7 +7,7 @@
  * program (or a cgo/ctypes binding) uses instead: the library owns the device memory
  * of a queue, callers hold an opaque handle, and the harness kernels of the four
  * reference harnesses are exposed as calls.  Device code that wants the per-thread
- * API links against include/gcq/*.cuh and gets the device-side queue from
+ * API links against the headers in include/gcq/ and gets the device-side queue from
  * gcq_device_ptr().
  *
  * Conventions: every call returns GCQ_OK (0) or a negative gcq_status; no call
@@ -86,7 +86,7 @@ int gcq_destroy(gcq_queue* q);
 /* Re-initialise on `stream` with a grid-stride kernel (the reference re-runs its
  * serial init, bfs_bench.cpp:531-552). */
 int gcq_reset(gcq_queue* q, void* stream);
-/* Device address of the queue object for kernels using include/gcq/*.cuh:
+/* Device address of the queue object for kernels using the headers in include/gcq/:
  * gcq::gwf::mpmc*, gcq::glf::mpmc*, gcq::ymc::queue* or gcq::sfq::queue*. */
 int gcq_device_ptr(gcq_queue* q, void** dev);
 /* Read (and optionally clear) the device error word; synchronises the device. */

@@ -85,3 +85,36 @@ def test_argument_checks_without_gpu(built_lib):
     L.gcq_serve_default_cfg(ctypes.byref(cfg))
     assert cfg.budget_bytes == 150 << 30 and cfg.rt_scenes == 0
     assert (cfg.rt_width, cfg.rt_height, cfg.rt_tile_px, cfg.rt_max_bounces, cfg.rt_slots) == (1024, 1024, 32, 4, 1024)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "gcq.h"
+int main(void) {
+    gcq_knobs k;
+    gcq_serve_cfg c;
+    gcq_rt_result r;
+    gcq_queue* q = 0;
+    gcq_default_knobs(&k);
+    gcq_serve_default_cfg(&c);
+    if (gcq_create(GCQ_GWFQ, 30, 64, &k, &q) != GCQ_EINVAL) return 2;
+    if (gcq_rt_bounce_render(GCQ_WFQ, 0, 64, 64, 32, 64, 4, 15, 1, 0, &r) != GCQ_EUNSUPPORTED) return 3;
+    printf("%s|%u|%u\n", gcq_strerror(GCQ_EINVAL), k.help_delay, c.rt_tile_px);
+    return 0;
+}
+"""
+
+
+def test_header_is_plain_c(built_lib, tmp_path):
+    """include/gcq.h compiles as strict C11 and a C caller links and runs against
+    libgcq.so (host-only calls: no GPU needed)."""
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    lib_dir = os.path.dirname(built_lib)
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    str(src), "-o", str(exe), "-L" + lib_dir, "-lgcq", "-Wl,-rpath," + lib_dir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out
+    assert out.stdout.strip() == "invalid argument|64|32"
