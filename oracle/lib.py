@@ -41,7 +41,9 @@ _LIB = None
 def lib():
     global _LIB
     if _LIB is None:
-        path = os.path.join(_build.OUT, "liboracle.so")
+        # GCQ_ORACLE_LIBRARY selects another build of the same sources (the
+        # ThreadSanitizer copy of the race tests)
+        path = os.environ.get("GCQ_ORACLE_LIBRARY") or os.path.join(_build.OUT, "liboracle.so")
         if not os.path.exists(path):
             path = _build.build()
         L = C.CDLL(path)
