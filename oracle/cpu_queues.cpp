@@ -1235,4 +1235,84 @@ int oracle_gwf_slow_passed_slot(int reference_rule, uint32_t* deq_out) {
     return done_at_T ? 1 : 0;
 }
 
+// Host fault injection for the wait-free helping of G-WFQ (gwf_ring.hpp:808-861,
+// restated above): thread 0 takes a Tail ticket, publishes a slow-path enqueue
+// request for index `stalled_index` and then stalls -- it makes no further step --
+// while `threads - 1` workers each run `ops` enqueue/dequeue pairs of their own
+// values with patience 1, so every operation takes the slow path, checking one peer
+// every `help_delay` operations (1: every operation; a delay longer than the run
+// disables helping, the control case).  The stalled request must be completed by the helpers: its
+// index reaches a worker's dequeue while thread 0 is still stalled.  Thread 0 then
+// resumes its own slow path, which must find the request done and not insert the
+// index again; a final drain must find every value exactly once.  Returns 1 when
+// all of that holds, 0 when it does not, negative for bad arguments.
+// stats[0]: dequeues of the stalled index by workers while thread 0 was stalled,
+// stats[1]: dequeues of it in total, stats[2]: worker values dequeued exactly once,
+// stats[3]: worker values enqueued.
+int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_delay, uint64_t* stats) {
+    if (threads < 2 || threads > 64 || ops == 0 || ops > 4096 || help_delay == 0 || !stats) return -1;
+    gwf::Ring q;
+    gwf::Knobs kn;
+    kn.help_delay = (int)help_delay;
+    kn.enq_patience = 1;
+    kn.deq_patience = 1;
+    q.init(1024, threads, bits_for(threads), kn);
+    const u32 stalled_index = 7;   // workers use values from 1000 up
+    // thread 0: a failed fast-path ticket, then the published request, then nothing
+    const u64 T = q.cnt_of(q.Tail.fetch_add(q.cinc));
+    gwf::Rec& r = q.Record[0];
+    const u32 seq = r.seq1.load();
+    r.localTail.store(T << 2);
+    r.initTail.store(T << 2);
+    r.index.store(stalled_index);
+    r.enqueue.store(1);
+    r.seq2.store(seq);
+    r.pending.store(1);
+    std::vector<std::vector<u32>> got(threads);
+    std::vector<std::thread> ths;
+    std::atomic<int> ready{0};
+    for (u32 w = 1; w < threads; ++w) {
+        ths.emplace_back([&, w]() {
+            ready.fetch_add(1);
+            while (ready.load() < (int)threads - 1) cpu_relax();
+            for (u32 i = 0; i < ops; ++i) {
+                q.enqueue_wf(1000 + w * ops + i, w);
+                const u32 v = q.dequeue_wf(w);
+                if (v != gwf::BOT) got[w].push_back(v);
+            }
+        });
+    }
+    for (auto& th : ths) th.join();
+    uint64_t seen_while_stalled = 0;
+    for (u32 w = 1; w < threads; ++w)
+        for (u32 v : got[w]) seen_while_stalled += (v == stalled_index);
+    // thread 0 resumes: its own slow path must find the request finished
+    q.enqueue_slow(T << 2, stalled_index, r, 0);
+    r.pending.store(0);
+    r.seq1.store(seq + 1);
+    std::vector<u32> all;
+    for (u32 w = 1; w < threads; ++w) all.insert(all.end(), got[w].begin(), got[w].end());
+    for (int k = 0; k < (int)(threads * ops + 16); ++k) {
+        const u32 v = q.dequeue_wf(0);
+        if (v == gwf::BOT) break;
+        all.push_back(v);
+    }
+    uint64_t stalled_total = 0, worker_once = 0;
+    std::vector<u32> counts((size_t)threads * ops + 1000, 0);
+    bool ok = true;
+    for (u32 v : all) {
+        if (v == stalled_index) { ++stalled_total; continue; }
+        if (v < 1000 || v - 1000 >= threads * ops) { ok = false; continue; }
+        ++counts[v - 1000];
+    }
+    const uint64_t enqueued = (uint64_t)(threads - 1) * ops;
+    for (u32 w = 1; w < threads; ++w)
+        for (u32 i = 0; i < ops; ++i) worker_once += counts[w * ops + i] == 1;
+    stats[0] = seen_while_stalled;
+    stats[1] = stalled_total;
+    stats[2] = worker_once;
+    stats[3] = enqueued;
+    return (ok && seen_while_stalled == 1 && stalled_total == 1 && worker_once == enqueued) ? 1 : 0;
+}
+
 }  // extern "C"

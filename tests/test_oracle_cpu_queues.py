@@ -52,3 +52,26 @@ def test_gwfq_slow_path_passed_slot(oracle_lib):
     assert out.value == 0xFFFFFFFE        # lost: the queue is empty
     assert oracle_lib.lib().oracle_gwf_slow_passed_slot(0, ctypes.byref(out)) == 0
     assert out.value == 5                 # delivered
+
+
+@pytest.mark.parametrize("threads, ops", [(2, 8), (8, 256), (32, 64)])
+def test_gwf_stalled_request_completed_by_helpers(oracle_lib, threads, ops):
+    """Host fault injection (wait-freedom of G-WFQ's helping, gwf_ring.hpp:808-861):
+    a thread that stalls right after publishing a slow-path enqueue has its index
+    inserted by the other threads while it is stalled, exactly once, and resuming
+    its own slow path afterwards inserts nothing more."""
+    import numpy as np
+    st = np.zeros(4, np.uint64)
+    assert oracle_lib.lib().oracle_gwf_stalled_helping(threads, ops, 1, st.ctypes.data) == 1
+    assert (int(st[0]), int(st[1])) == (1, 1)
+    assert st[2] == st[3] == (threads - 1) * ops
+
+
+def test_gwf_stalled_request_control_without_helping(oracle_lib):
+    """The control: with a help delay longer than the run nobody helps, so the
+    stalled index appears only after its own thread resumes."""
+    import numpy as np
+    st = np.zeros(4, np.uint64)
+    assert oracle_lib.lib().oracle_gwf_stalled_helping(8, 64, 1 << 20, st.ctypes.data) == 0
+    assert (int(st[0]), int(st[1])) == (0, 1)
+    assert st[2] == st[3]

@@ -1,7 +1,8 @@
 """Race detection on the CPU restatements of the four queues: the oracle's
 ThreadSanitizer build runs histories (alternating and split) and FIFO drains of
-every queue with 8 host threads; ThreadSanitizer must report nothing and every
-history must still check linearizable."""
+every queue with 8 host threads, and the stalled-thread helping case of G-WFQ;
+ThreadSanitizer must report nothing and every history must still check
+linearizable."""
 import os
 import subprocess
 import sys
@@ -18,6 +19,9 @@ for kind in ("gwfq", "glfq", "wfq", "sfq"):
         assert lib.check(h) == "Linearizable (FIFO)", (kind, mode)
     r = lib.cpu_fifo_check(kind, 8, 64)
     assert r["verified"] and r["dup"] == 0 and r["missing"] == 0, (kind, r)
+import numpy as np
+st = np.zeros(4, np.uint64)
+assert lib.lib().oracle_gwf_stalled_helping(8, 64, 1, st.ctypes.data) == 1, st
 print("ok")
 """
 
