@@ -206,6 +206,41 @@ constexpr uint64_t CELL_FULL = 1;
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// Signed max without a returned value (not waited for).
+__device__ __forceinline__ void red_max_rlx(int* p, int32_t v) {
+    asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Reset an SCQ Threshold to its maximum after a successful enqueue (SCQ's
+// "if Threshold != 3n-1 then Threshold = 3n-1"): a load of the hot word (served by
+// L2 for every lane of a warp at once) and an exchange only when it moved.  A
+// non-returning red.max in its place -- 3n-1 is the largest value the word holds,
+// so max is the exchange and the enqueuer would not wait for the load -- measured
+// 23.3 against 35.0 Gops/s (balanced G-WFQ, 262144 threads) and 21.1 against 61.7
+// (G-LFQ): every enqueue then sends an atomic to the one word, and the L2 slice
+// serialises them.
+__device__ __forceinline__ void reset_threshold(int* thr, int32_t thr_max) {
+    int32_t v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(thr) : "memory");
+    if (v != thr_max) {
+        int32_t old;
+        asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(thr), "r"(thr_max) : "memory");
+    }
+}
+
+// Order of an MPMC queue's index return to its free ring.  A consumer's last
+// access to a payload (its read or its take of a cell) must come before the next
+// producer's write to it.  The return carries a release -- a release CAS, or an
+// acq_rel fence followed by the CAS (a release pattern in the PTX memory model) --
+// and the producer obtains the index with an acquire read of the free ring's
+// entry, so under the PTX model the consumer's access precedes the producer's
+// write in causality order.  GCQ_ACQUIRE_ONLY_RETURN=1 makes the return
+// acquire-only: the consumer's access has then completed (its value returned)
+// before the CAS is issued, which orders it on this hardware, but the PTX model
+// gives no cross-thread order without the release.  Off by default.
+#ifndef GCQ_ACQUIRE_ONLY_RETURN
+#define GCQ_ACQUIRE_ONLY_RETURN 0
+#endif
 // CAS that reports success and refreshes `expect` with the observed value
 // (the C11 compare_exchange contract used by gwf_ring.hpp:93-99).
 __device__ __forceinline__ bool cas_upd(u64a* p, uint64_t* expect, uint64_t desired) {
@@ -320,6 +355,31 @@ __device__ __forceinline__ uint64_t warp_ticket(u64a* p, uint64_t step) {
     if ((int)lane_id() == leader) base = fetch_add_rlx(p, step * (uint64_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
     return base + (uint64_t)rank * step;
+}
+
+// A warp-aggregated ticket in two halves, so that the fetch-and-add's round trip
+// can overlap another memory access of the same lanes: ticket_issue sends the
+// leader's relaxed fetch-and-add and returns without waiting for it; the caller
+// issues its other access; ticket_take distributes the result (the first use of the
+// returned value, where the leader waits).  Both halves must run on the same lanes.
+struct ticket_req {
+    unsigned peers;
+    int leader;
+    unsigned rank;
+    uint64_t base;   // the leader's pending fetch-and-add result
+};
+__device__ __forceinline__ ticket_req ticket_issue(u64a* p, uint64_t step) {
+    ticket_req t;
+    const unsigned active = __activemask();
+    t.peers = __match_any_sync(active, (unsigned long long)(uintptr_t)p);
+    t.leader = __ffs(t.peers) - 1;
+    t.rank = __popc(t.peers & lanemask_lt());
+    t.base = 0;
+    if ((int)lane_id() == t.leader) t.base = fetch_add_rlx(p, step * (uint64_t)__popc(t.peers));
+    return t;
+}
+__device__ __forceinline__ uint64_t ticket_take(const ticket_req& t, uint64_t step) {
+    return __shfl_sync(t.peers, t.base, t.leader) + (uint64_t)t.rank * step;
 }
 
 // ---------------------------------------------------------------- waiting

@@ -143,7 +143,7 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
         // consumed); a mismatch returns the current value for the loop below.
         uint64_t E = ent::pack(tcyc - 1, true, BOT_C);
         if (cas_upd_ord<Publish>(&c.entry[j], &E, ent::pack(tcyc, true, index))) {
-            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            reset_threshold(&q->Threshold, c.threshold_max());
             return true;
         }
         for (;; ++spin) {
@@ -157,7 +157,7 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
                 if (spin >= GCQ_SPIN_LIMIT) break;
                 continue;
             }
-            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            reset_threshold(&q->Threshold, c.threshold_max());
             return true;
         }
     }
@@ -212,34 +212,97 @@ __device__ inline uint32_t dequeue(ring* q) {
 }
 
 // fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582.  The payload is written
-// before an acq_rel index enqueue and read with an acquire load, which orders the
-// index's return to fq after the read.  (Cells as in G-WFQ measured slower here:
-// 52.6 against 60.1 Gops/s balanced at 262144 threads.)
-__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) {
-    const uint32_t idx = dequeue(&q->fq);
+// before an acq_rel index enqueue (the release publishes it) and read after the
+// dequeue's acquire; the index's return to fq is an acq_rel CAS, whose release
+// orders the read before the next producer's write (GCQ_ACQUIRE_ONLY_RETURN).  (Cells
+// as in G-WFQ measured slower here: 52.6 against 60.1 Gops/s balanced at 262144
+// threads.)  They work on the two rings and the payload array, so the library's
+// queue (mpmc) and the self-contained fq_mpmc_t below run the same code.
+__device__ __forceinline__ bool enqueue_ptr(ring* aq, ring* fq, u64a* data, uint64_t value) {
+    const uint32_t idx = dequeue(fq);
     if (idx == BOT) return false;
-    st_rlx(&q->data[idx], value);
-    return enqueue(&q->aq, idx);
+    st_rlx(&data[idx], value);
+    return enqueue(aq, idx);
 }
-__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out) {
-    const uint32_t idx = dequeue(&q->aq);
+__device__ __forceinline__ bool dequeue_ptr(ring* aq, ring* fq, u64a* data, uint64_t* out) {
+    const uint32_t idx = dequeue(aq);
     if (idx == BOT) return false;
-    *out = ld_acq(&q->data[idx]);
-    enqueue<false>(&q->fq, idx);
+    *out = ld_acq(&data[idx]);
+    enqueue<!GCQ_ACQUIRE_ONLY_RETURN>(fq, idx);
     return true;
 }
+__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value) { return enqueue_ptr(&q->aq, &q->fq, q->data, value); }
+__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out) { return dequeue_ptr(&q->aq, &q->fq, q->data, out); }
 
 }  // namespace glf
 }  // namespace gcq
 
 // -----------------------------------------------------------------------------
-// Reference-named device API (glf_queue.hpp:418-582) over the runtime rings.
+// Reference-named device API (glf_queue.hpp:32-46, 126-138, 418-582).
+//
+// fq_ring_t and fq_mpmc_t are self-contained, as in the reference: a caller
+// allocates sizeof(fq_mpmc_t) and runs fq_init on one thread.  A ring is the
+// library's ring header (Tail, Head and Threshold GCQ_HOT_STRIDE apart, then the
+// parameters) followed by its FQ_SLOTS entries; fq_ring_init_* point the header at
+// them.  The payload array is the reference's data[FQ_N].
 // -----------------------------------------------------------------------------
-typedef gcq::glf::ring fq_ring_t;
-typedef gcq::glf::mpmc fq_mpmc_t;
+static constexpr uint32_t FQ_SLOTS = 2 * FQ_N;
+static constexpr int32_t FQ_THRESH_MAX = 3 * (int32_t)FQ_N - 1;
 static constexpr uint32_t FQ_BOT = gcq::glf::BOT;
 static constexpr uint32_t FQ_BOT_C = gcq::glf::BOT_C;
-__device__ __forceinline__ void fq_enqueue(fq_ring_t* q, uint32_t index) { gcq::glf::enqueue(q, index); }
-__device__ __forceinline__ uint32_t fq_dequeue(fq_ring_t* q) { return gcq::glf::dequeue(q); }
-__device__ __forceinline__ bool fq_enqueue_ptr(fq_mpmc_t* q, uint64_t v) { return gcq::glf::enqueue_ptr(q, v); }
-__device__ __forceinline__ bool fq_dequeue_ptr(fq_mpmc_t* q, uint64_t* out) { return gcq::glf::dequeue_ptr(q, out); }
+static_assert((FQ_N & (FQ_N - 1)) == 0, "FQ_N must be a power of two");
+
+struct fq_ring_t : gcq::glf::ring {
+    // The reference's Entry[FQ_SLOTS]; the header's own Entry pointer (gcq::glf::ring::Entry),
+    // hidden by this name, is set to it by the initialisers.
+    unsigned long long Entry[FQ_SLOTS];
+    gcq::u32a err_word;
+};
+struct fq_mpmc_t {
+    fq_ring_t aq;   // allocated indices
+    fq_ring_t fq;   // free indices
+    uint64_t data[FQ_N];
+};
+
+// fq_ring_init_empty / fq_ring_init_full, glf_queue.hpp:418-435 (one thread).
+__device__ inline void fq_ring_setup(fq_ring_t* q) {
+    gcq::glf::ring* h = q;
+    h->Entry = q->Entry;
+    q->err_word = 0;
+    h->err = &q->err_word;
+    h->order = 31 - __clz(FQ_N);
+#ifdef FQ_CACHE_REMAP
+    h->line_log2 = 3;   // the reference's cache_remap: 8 entries per 64-byte line (glf_queue.hpp:116-120)
+#else
+    h->line_log2 = 0;   // identity, the library's default (contiguous tickets coalesce in L2)
+#endif
+    h->deq_wait = 0;
+}
+__device__ inline void fq_ring_init_empty(fq_ring_t* q) {
+    fq_ring_setup(q);
+    gcq::glf::init_slice(q, false, 0, 1);
+    __threadfence();
+}
+__device__ inline void fq_ring_init_full(fq_ring_t* q) {
+    fq_ring_setup(q);
+    gcq::glf::init_slice(q, true, 0, 1);
+    __threadfence();
+}
+// fq_init, glf_queue.hpp:437-440
+__device__ inline void fq_init(fq_mpmc_t* q) {
+    fq_ring_init_empty(&q->aq);
+    fq_ring_init_full(&q->fq);
+}
+// fq_enqueue / fq_dequeue, glf_queue.hpp:467-560, on a self-contained ring or a
+// ring header of the library's queues (gcq::glf::ring).
+__device__ __forceinline__ void fq_enqueue(gcq::glf::ring* q, uint32_t index) { gcq::glf::enqueue(q, index); }
+__device__ __forceinline__ uint32_t fq_dequeue(gcq::glf::ring* q) { return gcq::glf::dequeue(q); }
+// fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582
+__device__ __forceinline__ bool fq_enqueue_ptr(fq_mpmc_t* q, uint64_t v) {
+    return gcq::glf::enqueue_ptr(&q->aq, &q->fq, (gcq::u64a*)q->data, v);
+}
+__device__ __forceinline__ bool fq_dequeue_ptr(fq_mpmc_t* q, uint64_t* out) {
+    return gcq::glf::dequeue_ptr(&q->aq, &q->fq, (gcq::u64a*)q->data, out);
+}
+__device__ __forceinline__ bool fq_enqueue_ptr(gcq::glf::mpmc* q, uint64_t v) { return gcq::glf::enqueue_ptr(q, v); }
+__device__ __forceinline__ bool fq_dequeue_ptr(gcq::glf::mpmc* q, uint64_t* out) { return gcq::glf::dequeue_ptr(q, out); }

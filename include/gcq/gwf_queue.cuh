@@ -260,10 +260,14 @@ struct wf_t {
     gcq::u32a Owner[SLOTS];
 };
 
+// Indirection queue (gwf_queue.hpp:338-345) as one object a caller can allocate
+// with sizeof and initialise with wf_mpmc_init.  The payloads are cells of 16 bytes
+// ({value, full}, the library's layout) instead of the reference's 8-byte data[N]:
+// Enqueue_Ptr/Dequeue_Ptr run the library's code on it.
 template <typename Config, uint32_t N_PARAM>
 struct wf_mpmc_t {
     using queue_type = wf_t<Config, N_PARAM>;
     queue_type aq;
     queue_type fq;
-    uint64_t data[N_PARAM];
+    gcq::cell data[N_PARAM];
 };

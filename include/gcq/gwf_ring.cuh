@@ -111,16 +111,16 @@ __device__ inline void catchup(ring* q, const cfg& c, uint64_t tail_raw, uint64_
 }
 
 // ------------------------------------------------------------------ fast path
-// try_enq, gwf_ring.hpp:382-414.  0 on success, else the ticket tried.
+// try_enq, gwf_ring.hpp:382-414, on ticket T (a Tail counter value).  0 on
+// success, else T.
 // Publish: the caller wrote what the index refers to before this call, and the
 // entry CAS is acq_rel -- release orders those writes before the index, acquire
-// orders the Threshold read after the CAS.  Without Publish the caller has ordered
-// its earlier accesses itself (with an acquire load), and the CAS is acquire only:
-// a release costs a further L2 round trip, an acquire nothing measurable.
+// orders the Threshold reset after the CAS.  Without Publish the caller has ordered
+// its earlier accesses itself, and the CAS is acquire only: a release costs a
+// further L2 round trip on this GPU, an acquire nothing measurable.
 template <bool Publish = true>
-__device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
+__device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uint64_t T) {
     GCQ_STAT(c, stat::TRY_ENQ);
-    const uint64_t T = c.counter(warp_ticket(&q->Tail, c.cinc()));
     const uint32_t tcyc = c.cycle_of(T);
     const uint32_t j = c.slot_of(T);
     // In steady state the slot holds the previous cycle's consumed entry (Note
@@ -130,7 +130,7 @@ __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
     // have read, so the code below continues from it.  Saves one L2 round trip.
     uint64_t E = entry::pack(0xFF, tcyc - 1, true, true, BOT_C);
     if (cas_upd_ord<Publish>(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
-        if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+        reset_threshold(&q->Threshold, c.threshold_max());
         return 0;
     }
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
@@ -143,21 +143,49 @@ __device__ inline uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
         }
         const uint64_t nw = entry::pack(entry::note(E), tcyc, true, true, index);
         if (!cas_upd_ord<Publish>(&c.entry[j], &E, nw)) continue;
-        if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+        reset_threshold(&q->Threshold, c.threshold_max());
         return 0;
     }
     raise_error(c.err, ERR_SPIN);
     return T;
 }
+template <bool Publish = true>
+__device__ __forceinline__ uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
+    return try_enq_at<Publish>(q, c, index, c.counter(warp_ticket(&q->Tail, c.cinc())));
+}
+
+// An enqueue ticket taken ahead of need and then not used (the operation it was for
+// found the queue full): the slot is marked passed at the ticket's cycle, as the
+// dequeuer holding the same ticket would mark it, so that dequeuer does not wait
+// for an index that will not come.  A slot holding an older index is left for that
+// dequeuer.  Not waited for; a failed CAS means the slot moved on and needs nothing.
+__device__ inline void abandon_enq_ticket(ring* q, uint64_t T_raw) {
+    const cfg c = load_cfg(q);
+    const uint64_t T = c.counter(T_raw);
+    const uint32_t tcyc = c.cycle_of(T);
+    const uint32_t j = c.slot_of(T);
+    const uint64_t E = ld_rlx(&c.entry[j]);
+    if (cycle_cmp(entry::cycle(E), tcyc) < 0 && entry::empty_index(entry::index(E)))
+        cas_rlx(&c.entry[j], E, entry::pack(entry::note(E), tcyc, entry::safe(E), true, BOT));
+}
 
 // try_deq, gwf_ring.hpp:421-472.  0 when finished (*out = index, or BOT if the
 // queue is empty), else the ticket tried.
-__device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_t tid) {
+// With PF the same lanes also take a ticket of the counter pf_ctr (another ring's
+// Tail, for the enqueue that follows this dequeue): its fetch-and-add is issued
+// together with this ticket's slot load, so its round trip overlaps the load's;
+// *pf_raw receives the raw counter word.
+template <bool PF = false>
+__device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_t tid, u64a* pf_ctr = nullptr,
+                                   uint64_t* pf_raw = nullptr) {
     GCQ_STAT(c, stat::TRY_DEQ);
     const uint64_t H = c.counter(warp_ticket(&q->Head, c.cinc()));
     const uint32_t hcyc = c.cycle_of(H);
     const uint32_t j = c.slot_of(H);
+    ticket_req pf;
+    if (PF) pf = ticket_issue(pf_ctr, c.cinc());
     uint64_t E = ld_acq(&c.entry[j]);   // acquire: see consume
+    if (PF) *pf_raw = ticket_take(pf, c.cinc());
     // The slot of an earlier cycle with no index: the enqueuer holding this ticket
     // may be about to fill it.  Marking it now would make that enqueuer retry with a
     // new ticket, and this dequeuer too; re-reading it a few times first (bounded,
@@ -299,7 +327,7 @@ __device__ inline bool try_enq_slow(ring* q, const cfg& c, uint64_t T_raw, uint3
             const uint64_t T_local = T_raw << 2;
             if (cas_ok(&r->localTail, T_local, T_local | local::FIN))
                 cas(&c.entry[j], nn, entry::pack(enote, tcyc, true, true, index));
-            if (ld_rlx(&q->Threshold) != c.threshold_max()) exchange(&q->Threshold, c.threshold_max());
+            reset_threshold(&q->Threshold, c.threshold_max());
             return true;
         }
         // The slot is at our cycle: produced for this request (our index, or
@@ -405,16 +433,31 @@ __device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid
 }
 
 // ------------------------------------------------------------------ top level
-// Enqueue_wf, gwf_ring.hpp:1234-1284 (Publish: see try_enq)
-template <bool Publish = true>
-__device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
+// Enqueue_wf, gwf_ring.hpp:1234-1284 (Publish: see try_enq).  first_raw, when
+// not 0, is a Tail ticket the caller already took (try_deq's prefetch): the first
+// fast-path attempt uses it.  Tickets start at 2N, so 0 never names one.
+// HelpAfter moves the operation's help check (help_threads) from before its own
+// work to after it.  A release CAS waits for every earlier write of the thread, and
+// the help check writes the thread's countdown: after the CAS, that store is not
+// waited for.  Each operation still makes one help check, so a peer's request is
+// still visited within help_delay operations of every thread.
+template <bool Publish = true, bool HelpAfter = false>
+__device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t first_raw = 0) {
     const cfg c = load_cfg(q);
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return; }
-    help_threads(q, c, tid);
+    if (!HelpAfter) help_threads(q, c, tid);
     uint64_t tail = 0;
     for (uint32_t count = c.enq_patience; --count != 0;) {
-        tail = try_enq<Publish>(q, c, index);
-        if (tail == 0) return;
+        if (first_raw) {
+            tail = try_enq_at<Publish>(q, c, index, c.counter(first_raw));
+            first_raw = 0;
+        } else {
+            tail = try_enq<Publish>(q, c, index);
+        }
+        if (tail == 0) {
+            if (HelpAfter) help_threads(q, c, tid);
+            return;
+        }
     }
     GCQ_STAT(c, stat::ENQ_SLOW);
     record* r = &c.rec[tid];
@@ -429,17 +472,25 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid) {
     enqueue_slow(q, c, tail_local, index, r, tid);
     st_rel(&r->pending, 0u);
     st_rel(&r->seq1, seq + 1);
+    if (HelpAfter) help_threads(q, c, tid);
 }
 
 // Dequeue_wf, gwf_ring.hpp:1286-1356.  Returns the index or BOT when empty.
-__device__ inline uint32_t dequeue(ring* q, uint32_t tid) {
+// With PF the first fast-path attempt also takes a ticket of pf_ctr into *pf_raw
+// (see try_deq); *pf_raw stays 0 when the dequeue returns before taking one.
+template <bool PF = false>
+__device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr, uint64_t* pf_raw = nullptr) {
     const cfg c = load_cfg(q);
     if (ld_rlx(&q->Threshold) < 0) return BOT;
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return BOT; }
     help_threads(q, c, tid);
     uint32_t out = BOT;
     uint64_t head = 0;
-    for (uint32_t count = c.deq_patience; --count != 0;) {
+    if (PF) {
+        head = try_deq<true>(q, c, &out, tid, pf_ctr, pf_raw);
+        if (head == 0) return out;
+    }
+    for (uint32_t count = c.deq_patience - (PF ? 1u : 0u); --count != 0;) {
         head = try_deq(q, c, &out, tid);
         if (head == 0) return out;
     }
@@ -492,22 +543,89 @@ __device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
     return BOT;
 }
 
-// Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.  The
-// payload travels in a cell (put_cell / take_cell), so both index enqueues are
-// acquire-only.
-__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
-    const uint32_t idx = dequeue(&q->fq, tid);
+// Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.
+// The payload travels in a cell (put_cell / take_cell), so the index's enqueue to
+// aq publishes nothing and is acquire-only; its return to fq carries a release
+// (it orders the take before the next producer's put; see take_and_return).
+// With GCQ_TICKET_PREFETCH (default) each operation takes its second ring's ticket
+// while the first ring's access is in flight: Enqueue_Ptr issues the aq Tail
+// fetch-and-add beside the fq slot load, Dequeue_Ptr issues the fq Tail
+// fetch-and-add beside the cell's take.  Each saves one dependent L2 round trip.
+//
+// The operations work on a view of an indirection queue -- its two rings, its
+// cells and its error word -- so the library's queue (mpmc) and the compile-time
+// wf_mpmc_t below run the same code.
+#ifndef GCQ_TICKET_PREFETCH
+#define GCQ_TICKET_PREFETCH 1
+#endif
+struct mpmc_view {
+    ring* aq;
+    ring* fq;
+    cell* data;
+    u32a* err;
+};
+__device__ __forceinline__ mpmc_view view_of(mpmc* q) { return mpmc_view{&q->aq, &q->fq, q->data, q->err}; }
+
+__device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, uint32_t tid) {
+#if GCQ_TICKET_PREFETCH
+    uint64_t aq_raw = 0;
+    const uint32_t idx = dequeue<true>(q.fq, tid, &q.aq->Tail, &aq_raw);
+    if (idx == BOT) {
+        if (aq_raw) abandon_enq_ticket(q.aq, aq_raw);
+        return false;
+    }
+    put_cell(&q.data[idx], value);
+    enqueue<false>(q.aq, idx, tid, aq_raw);
+#else
+    const uint32_t idx = dequeue(q.fq, tid);
     if (idx == BOT) return false;
-    put_cell(&q->data[idx], value);
-    enqueue<false>(&q->aq, idx, tid);
+    put_cell(&q.data[idx], value);
+    enqueue<false>(q.aq, idx, tid);
+#endif
     return true;
 }
-__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid) {
-    const uint32_t idx = dequeue(&q->aq, tid);
+// Take the cell of index idx and return idx to fq.  The return's release is an
+// acq_rel fence issued as soon as the take has returned (GCQ_RETURN_FENCE, the
+// default), before the enqueue's help bookkeeping writes anything: the fence then
+// waits only for accesses already complete or in flight beside the take, where a
+// release CAS after that bookkeeping waits for its store too.
+#ifndef GCQ_RETURN_FENCE
+#define GCQ_RETURN_FENCE 0
+#endif
+#ifndef GCQ_RETURN_HELP_AFTER
+#define GCQ_RETURN_HELP_AFTER 1
+#endif
+__device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t idx, uint32_t tid) {
+#if GCQ_TICKET_PREFETCH
+    const uint64_t inc = 1ULL << q.fq->thr_bits;
+    const ticket_req t = ticket_issue(&q.fq->Tail, inc);
+    uint64_t v, f;
+    exch128<true>(&q.data[idx].value, 0, 0, &v, &f);
+    const uint64_t fq_raw = ticket_take(t, inc);
+    if (f != CELL_FULL) v = take_cell(&q.data[idx], q.err);
+#else
+    const uint64_t v = take_cell(&q.data[idx], q.err);
+    const uint64_t fq_raw = 0;
+#endif
+#if GCQ_RETURN_FENCE
+    if (!GCQ_ACQUIRE_ONLY_RETURN) fence_acq_rel();
+    enqueue<false>(q.fq, idx, tid, fq_raw);
+#else
+    enqueue<!GCQ_ACQUIRE_ONLY_RETURN, GCQ_RETURN_HELP_AFTER>(q.fq, idx, tid, fq_raw);
+#endif
+    return v;
+}
+__device__ __forceinline__ bool dequeue_ptr(const mpmc_view& q, uint64_t* out, uint32_t tid) {
+    const uint32_t idx = dequeue(q.aq, tid);
     if (idx == BOT) return false;
-    *out = take_cell(&q->data[idx], q->err);
-    enqueue<false>(&q->fq, idx, tid);
+    *out = take_and_return(q, idx, tid);
     return true;
+}
+__device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
+    return enqueue_ptr(view_of(q), value, tid);
+}
+__device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid) {
+    return dequeue_ptr(view_of(q), out, tid);
 }
 // Enqueue for workloads whose consumers poll (the reference has none): fast-path
 // attempts only.  With many pollers a request on the wait-free slow path does not
@@ -530,8 +648,7 @@ __device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t ti
 __device__ __forceinline__ bool try_dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->aq, tid, tries);
     if (idx == BOT) return false;
-    *out = take_cell(&q->data[idx], q->err);
-    enqueue<false>(&q->fq, idx, tid);
+    *out = take_and_return(view_of(q), idx, tid);
     return true;
 }
 
@@ -547,7 +664,9 @@ __device__ __forceinline__ uint32_t wf_tid() { return (uint32_t)(WF_TID_EXPR); }
 __device__ __forceinline__ uint32_t wf_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 #endif
 
-// Serial single-thread initialisation, as the reference's <<<1,1>>> init kernels do.
+// Serial single-thread initialisation, as the reference's <<<1,1>>> init kernels do
+// (wf_init, gwf_ring.hpp:229-276; full = the free-index ring of wf_mpmc_init,
+// :278-298).  The ring header points at the arrays of the same object.
 template <typename Config, uint32_t N_PARAM>
 __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
     gcq::gwf::ring* h = &q->hdr;
@@ -571,32 +690,17 @@ __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
     h->deq_wait = 0;
     h->stats = nullptr;
     __threadfence();
-    // single thread: the slice covers the whole ring (no block sync needed
-    // because gid 0 of a 1-thread group owns every element)
-    const gcq::gwf::cfg c = gcq::gwf::load_cfg(h);
-    for (uint32_t i = 0; i < c.slots(); ++i) { c.entry[i] = gcq::gwf::entry::INIT; c.owner[i] = 0; }
-    if (full)
-        for (uint32_t i = 0; i < N_PARAM; ++i) {
-            const uint64_t t = (uint64_t)c.slots() + i;
-            c.entry[c.slot_of(t)] = gcq::gwf::entry::pack(0xFF, c.cycle_of(t), true, true, i);
-        }
-    for (uint32_t i = 0; i < c.max_threads; ++i) {
-        gcq::gwf::record* r = &c.rec[i];
-        r->seq1 = 1; r->enqueue = 0; r->pending = 0; r->index = 0;
-        r->localTail = 0; r->initTail = 0; r->localHead = 0; r->initHead = 0; r->seq2 = 0;
-        r->p2_seq1 = 1; r->p2_local = 0; r->p2_cnt = 0; r->p2_seq2 = 0;
-        c.help[i].nextCheck = (int32_t)c.help_delay;
-        c.help[i].nextTid = i;
-    }
-    h->Head = c.pack_global(c.slots(), c.null_tid());
-    h->Tail = c.pack_global(full ? c.slots() + N_PARAM : c.slots(), c.null_tid());
-    h->Threshold = full ? c.threshold_max() : -1;
+    // one thread covers the whole ring (a grid-stride slice of width 1)
+    gcq::gwf::init_slice(h, full, 0, 1);
     __threadfence();
 }
+// wf_mpmc_init, gwf_ring.hpp:278-298: aq empty, fq holding 0..N-1, every cell empty.
 template <typename Config, uint32_t N_PARAM>
 __device__ void wf_mpmc_init(wf_mpmc_t<Config, N_PARAM>* q) {
     wf_init(&q->aq, false);
     wf_init(&q->fq, true);
+    for (uint32_t i = 0; i < N_PARAM; ++i) { q->data[i].value = 0; q->data[i].full = 0; }
+    __threadfence();
 }
 template <typename Config, uint32_t N_PARAM>
 __device__ __forceinline__ void Enqueue_wf(wf_t<Config, N_PARAM>* q, uint32_t index) {
@@ -607,20 +711,14 @@ __device__ __forceinline__ uint32_t Dequeue_wf(wf_t<Config, N_PARAM>* q) {
     return gcq::gwf::dequeue(&q->hdr, wf_tid());
 }
 template <typename Config, uint32_t N_PARAM>
+__device__ __forceinline__ gcq::gwf::mpmc_view wf_view(wf_mpmc_t<Config, N_PARAM>* q) {
+    return gcq::gwf::mpmc_view{&q->aq.hdr, &q->fq.hdr, q->data, &q->aq.err};
+}
+template <typename Config, uint32_t N_PARAM>
 __device__ __forceinline__ bool Enqueue_Ptr(wf_mpmc_t<Config, N_PARAM>* q, uint64_t value) {
-    const uint32_t tid = wf_tid();
-    const uint32_t idx = gcq::gwf::dequeue(&q->fq.hdr, tid);
-    if (idx == gcq::gwf::BOT) return false;
-    gcq::st_rlx((gcq::u64a*)&q->data[idx], value);
-    gcq::gwf::enqueue(&q->aq.hdr, idx, tid);
-    return true;
+    return gcq::gwf::enqueue_ptr(wf_view(q), value, wf_tid());
 }
 template <typename Config, uint32_t N_PARAM>
 __device__ __forceinline__ bool Dequeue_Ptr(wf_mpmc_t<Config, N_PARAM>* q, uint64_t* out) {
-    const uint32_t tid = wf_tid();
-    const uint32_t idx = gcq::gwf::dequeue(&q->aq.hdr, tid);
-    if (idx == gcq::gwf::BOT) return false;
-    *out = gcq::ld_rlx((const gcq::u64a*)&q->data[idx]);
-    gcq::gwf::enqueue(&q->fq.hdr, idx, tid);
-    return true;
+    return gcq::gwf::dequeue_ptr(wf_view(q), out, wf_tid());
 }

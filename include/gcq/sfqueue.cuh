@@ -163,23 +163,90 @@ __device__ inline int dequeue_nb(queue* q, uint32_t* out) {
 }  // namespace gcq
 
 // -----------------------------------------------------------------------------
-// Reference-named device API (sfqueue_hip.hpp:68-83).
+// Reference-named device and host API (sfqueue_hip.hpp:13-102, sfqueue_hip.cpp:130-180,
+// 356-399).
+//
+// sfq_queue is self-contained, as in the reference: the library's queue header
+// (head, tail and closed GCQ_HOT_STRIDE apart, then the parameters) followed by
+// SFQ_QUEUE_LENGTH slot words, each the reference's ids[i] and items[i] in one
+// 64-bit word.  head, tail, closed and nprocs keep the reference's names.
 // -----------------------------------------------------------------------------
-typedef gcq::sfq::queue sfq_queue;
+#ifndef SFQ_MAX_THREADS
+#define SFQ_MAX_THREADS 65535u
+#endif
+#define SFQ_GET_ID(x) (((x) / SFQ_QUEUE_LENGTH) * 2u)
+#define SFQ_MAX_ID (2u * ((UINT32_MAX / SFQ_QUEUE_LENGTH) + 1u))
+static_assert((SFQ_QUEUE_LENGTH & (SFQ_QUEUE_LENGTH - 1u)) == 0, "SFQ_QUEUE_LENGTH must be a power of two.");
+static_assert(SFQ_MAX_ID >= 2u * (SFQ_MAX_THREADS + 1u),
+              "SFQ_MAX_ID invariant violated: reduce SFQ_MAX_THREADS or queue length.");
+#ifndef SFQ_WAIT_TIMEOUT_NS
+#define SFQ_WAIT_TIMEOUT_NS 2000000000ull   // deadline of one blocking wait
+#endif
+
+struct sfq_queue : gcq::sfq::queue {
+    gcq::u64a slots[SFQ_QUEUE_LENGTH];
+    gcq::u32a err_word;
+};
 struct sfq_handle { uint32_t thread_id; uint32_t dummy[15]; };
-__device__ __forceinline__ int sfq_enqueue_blocking_u32(sfq_queue* q, uint32_t item) { return gcq::sfq::enqueue_blocking(q, item); }
-__device__ __forceinline__ int sfq_dequeue_blocking_u32(sfq_queue* q, uint32_t* out) { return gcq::sfq::dequeue_blocking(q, out); }
-__device__ __forceinline__ int sfq_enqueue_nb_u32(sfq_queue* q, uint32_t item) { return gcq::sfq::enqueue_nb(q, item); }
-__device__ __forceinline__ int sfq_dequeue_nb_u32(sfq_queue* q, uint32_t* out) { return gcq::sfq::dequeue_nb(q, out); }
-__device__ __forceinline__ void sfq_close(sfq_queue* q) { gcq::sfq::close(q); }
-__device__ __forceinline__ int sfq_is_closed(const sfq_queue* q) { return gcq::sfq::is_closed(q) ? 1 : 0; }
-// u64 wrapper: payload 0 is reserved for SFQ_EMPTY (sfqueue_hip.cpp:134-144)
-__device__ __forceinline__ void sfq_enqueue(sfq_queue* q, sfq_handle*, uint64_t v) {
+
+__device__ __forceinline__ int sfq_enqueue_blocking_u32(gcq::sfq::queue* q, uint32_t item) { return gcq::sfq::enqueue_blocking(q, item); }
+__device__ __forceinline__ int sfq_dequeue_blocking_u32(gcq::sfq::queue* q, uint32_t* out) { return gcq::sfq::dequeue_blocking(q, out); }
+__device__ __forceinline__ int sfq_enqueue_nb_u32(gcq::sfq::queue* q, uint32_t item) { return gcq::sfq::enqueue_nb(q, item); }
+__device__ __forceinline__ int sfq_dequeue_nb_u32(gcq::sfq::queue* q, uint32_t* out) { return gcq::sfq::dequeue_nb(q, out); }
+__device__ __forceinline__ void sfq_close(gcq::sfq::queue* q) { gcq::sfq::close(q); }
+__device__ __forceinline__ int sfq_is_closed(const gcq::sfq::queue* q) { return gcq::sfq::is_closed(q) ? 1 : 0; }
+// u64 wrapper: payload 0 is reserved for SFQ_EMPTY (sfqueue_hip.cpp:130-144)
+__device__ __forceinline__ void sfq_enqueue(gcq::sfq::queue* q, sfq_handle*, uint64_t v) {
     uint32_t item = (uint32_t)v;
     if (item == 0u) item = 1u;
     (void)gcq::sfq::enqueue_blocking(q, item);
 }
-__device__ __forceinline__ uint64_t sfq_dequeue(sfq_queue* q, sfq_handle*) {
+__device__ __forceinline__ uint64_t sfq_dequeue(gcq::sfq::queue* q, sfq_handle*) {
     uint32_t item = 0;
     return gcq::sfq::dequeue_blocking(q, &item) == SFQ_SUCCESS ? (uint64_t)item : SFQ_EMPTY;
+}
+
+// sfq_queue_init / sfq_handle_init, sfqueue_hip.cpp:150-162 (one thread; the slots
+// are cleared by sfq_init_kernel).
+__device__ inline void sfq_queue_init(sfq_queue* q, uint32_t nprocs) {
+    q->head = 0u;
+    q->tail = 0u;
+    q->closed = 0u;
+    q->slot = q->slots;
+    q->err_word = 0u;
+    q->err = &q->err_word;
+    q->log2_len = 31 - __clz(SFQ_QUEUE_LENGTH);
+    q->max_id = SFQ_MAX_ID;
+    q->timeout_ns = SFQ_WAIT_TIMEOUT_NS;
+    q->nprocs = nprocs;
+}
+__device__ inline void sfq_handle_init(sfq_handle* h, uint32_t tid) {
+    h->thread_id = tid;
+    for (int i = 0; i < 15; ++i) h->dummy[i] = 0u;
+}
+// sfq_init_kernel, sfqueue_hip.cpp:164-180
+static __global__ void sfq_init_kernel(sfq_queue* q, sfq_handle* handles, int num_threads) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = blockDim.x * gridDim.x;
+    if (tid == 0) sfq_queue_init(q, (uint32_t)num_threads);
+    for (int i = tid; i < (int)SFQ_QUEUE_LENGTH; i += total) q->slots[i] = 0;
+    for (int i = tid; i < num_threads; i += total) sfq_handle_init(&handles[i], (uint32_t)i);
+}
+// sfq_queue_host_init / sfq_queue_destroy, sfqueue_hip.cpp:356-399.  The reference
+// aborts the process on an error; this returns the CUDA error instead.
+static inline cudaError_t sfq_queue_host_init(sfq_queue** d_q, sfq_handle** d_handles, int num_threads) {
+    if (!d_q || !d_handles || num_threads < 0 || (uint32_t)num_threads > SFQ_MAX_THREADS) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMalloc((void**)d_q, sizeof(sfq_queue));
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc((void**)d_handles, (size_t)(num_threads > 0 ? num_threads : 1) * sizeof(sfq_handle));
+    if (e != cudaSuccess) { cudaFree(*d_q); return e; }
+    const int threads = 256;
+    const int blocks = num_threads > 0 ? (num_threads + threads - 1) / threads : 1;
+    sfq_init_kernel<<<blocks, threads>>>(*d_q, *d_handles, num_threads);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+static inline void sfq_queue_destroy(sfq_queue* d_q, sfq_handle* d_h) {
+    if (d_q) cudaFree(d_q);
+    if (d_h) cudaFree(d_h);
 }

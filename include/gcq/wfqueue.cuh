@@ -22,6 +22,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <string.h>
 #include "gcq_atomics.cuh"
 
 #ifndef WF_SEGMENT_SIZE
@@ -331,8 +332,143 @@ __device__ inline uint64_t dequeue(queue* q, uint32_t hid) {
 }  // namespace ymc
 }  // namespace gcq
 
-// Reference-named device API (wfqueue_hip_opt.hpp:527-555).  The handle argument
-// is the caller's handle index in this build.
+// -----------------------------------------------------------------------------
+// Reference-named device and host API (wfqueue_hip_opt.hpp:161-189, 527-764).
+//
+// wf_queue is the library's queue object and wf_handle its per-thread handle; a
+// handle passed to wf_enqueue/wf_dequeue must be an element of the array the queue
+// was initialised with (wf_init_kernel), which is how the reference's harnesses
+// use them (&handles[tid]).  The host helpers allocate the queue object, its error
+// word and its cell pool in one cudaMalloc, and the handles in another, as the
+// reference allocates the queue and the handles apart; the pool is device memory,
+// not managed memory (the reference's hipMallocManaged + prefetch,
+// wfqueue_hip_opt.hpp:604-640).  They return the first failing CUDA call's error
+// instead of printing, and the reference's pool sizes: threads * (3 * ops + 128)
+// cells plus WF_SEGMENT_SAFETY segments, or for BFS 1.2 * (V + E / chunk) + 10000
+// cells plus the same spare.
+// -----------------------------------------------------------------------------
 typedef gcq::ymc::queue wf_queue;
-__device__ __forceinline__ bool wf_enqueue(wf_queue* q, uint32_t h, uint64_t value) { return gcq::ymc::enqueue(q, h, value); }
-__device__ __forceinline__ uint64_t wf_dequeue(wf_queue* q, uint32_t h) { return gcq::ymc::dequeue(q, h); }
+typedef gcq::ymc::handle wf_handle;
+
+// wf_enqueue, wfqueue_hip_opt.hpp:527-536.  `value` must not be 0, ~0 or ~0-1.
+__device__ __forceinline__ bool wf_enqueue(wf_queue* q, wf_handle* h, uint64_t value) {
+    return gcq::ymc::enqueue(q, (uint32_t)(h - q->handles), value);
+}
+// wf_dequeue, wfqueue_hip_opt.hpp:538-555.  WF_EMPTY (0) when empty.
+__device__ __forceinline__ uint64_t wf_dequeue(wf_queue* q, wf_handle* h) {
+    return gcq::ymc::dequeue(q, (uint32_t)(h - q->handles));
+}
+// wf_dequeue_bfs, wfqueue_hip_opt.hpp:557-568: fast-path attempts only, giving up
+// as soon as the queue looks empty (T <= H + 1); no slow path, no helping.
+__device__ inline uint64_t wf_dequeue_bfs(wf_queue* q, wf_handle* h) {
+    const gcq::ymc::ctx x = gcq::ymc::load_ctx(q);
+    const uint32_t hid = (uint32_t)(h - q->handles);
+    uint64_t cid = 0;
+    for (int p = (int)q->patience; p >= 0; --p) {
+        const uint64_t v = gcq::ymc::deq_fast(x, hid, &cid);
+        if (v != gcq::ymc::RETRY) return v;
+        if (gcq::ld_acq(&q->T) <= gcq::ld_acq(&q->H) + 1) return WF_EMPTY;
+    }
+    return WF_EMPTY;
+}
+
+// wf_init_kernel, wfqueue_hip_opt.hpp:571-591: handle i links to handle i + 1 (mod
+// num_threads); thread 0 records the array in the queue.
+static __global__ void wf_init_kernel(wf_queue* q, wf_handle* handles, int num_threads) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        q->handles = handles;
+        q->nhandles = (uint32_t)num_threads;
+    }
+    if (tid >= num_threads) return;
+    wf_handle* h = &handles[tid];
+    h->enq_val = 0; h->enq_state = gcq::ymc::pack_state(0, 0);
+    h->deq_id = 0; h->deq_state = gcq::ymc::pack_state(0, 0);
+    h->next = (uint32_t)((tid + 1) % num_threads);
+    h->enq_peer = h->next;
+    h->deq_peer = h->next;
+    h->_pad = 0;
+    h->enq_id_last = 0;
+}
+
+// wf_clear_pool_kernel, wfqueue_hip_opt.hpp:646-663: clear the cells an operation
+// can have touched -- every cell below max(T, H) + 1 (the reference clears its
+// active segments).
+static __global__ void wf_clear_pool_kernel(wf_queue* q) {
+    const uint64_t t = q->T, hh = q->H;
+    const uint64_t span = (t > hh ? t : hh) + 1;
+    const uint64_t used = span < q->cap_cells ? span : q->cap_cells;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < used; i += (uint64_t)gridDim.x * blockDim.x) {
+        gcq::ymc::cell* c = &q->cells[i];
+        c->val = gcq::ymc::BOTTOM; c->enq = gcq::ymc::REQ_NULL; c->deq = gcq::ymc::REQ_NULL; c->_pad = 0;
+    }
+}
+
+static inline cudaError_t wf_queue_host_alloc(wf_queue** d_q, wf_handle** d_handles, int num_threads,
+                                              uint64_t cells) {
+    if (!d_q || !d_handles || num_threads <= 0) return cudaErrorInvalidValue;
+    cells += (uint64_t)WF_SEGMENT_SAFETY * WF_SEGMENT_SIZE;
+    const uint64_t head_bytes = (sizeof(wf_queue) + 255) / 256 * 256;
+    const uint64_t bytes = head_bytes + 256 + cells * sizeof(gcq::ymc::cell);
+    char* base = nullptr;
+    cudaError_t e = cudaMalloc((void**)&base, bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc((void**)d_handles, sizeof(wf_handle) * (size_t)num_threads);
+    if (e != cudaSuccess) { cudaFree(base); return e; }
+    wf_queue h;
+    memset(&h, 0, sizeof h);
+    h.cells = (gcq::ymc::cell*)(base + head_bytes + 256);
+    h.err = (gcq::u32a*)(base + head_bytes);
+    h.handles = *d_handles;
+    h.cap_cells = cells;
+    h.nhandles = (uint32_t)num_threads;
+    h.patience = WF_PATIENCE;
+    if ((e = cudaMemcpy(base, &h, sizeof h, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(base + head_bytes, 0, 256 + cells * sizeof(gcq::ymc::cell))) != cudaSuccess) {
+        cudaFree(*d_handles);
+        cudaFree(base);
+        return e;
+    }
+    *d_q = (wf_queue*)base;
+    const int block = 256;
+    wf_init_kernel<<<(num_threads + block - 1) / block, block>>>(*d_q, *d_handles, num_threads);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+// wf_queue_host_init_ex, wfqueue_hip_opt.hpp:594-644
+static inline cudaError_t wf_queue_host_init_ex(wf_queue** d_q, wf_handle** d_handles, int num_threads,
+                                                int ops_per_thread) {
+    if (ops_per_thread < 0) return cudaErrorInvalidValue;
+    return wf_queue_host_alloc(d_q, d_handles, num_threads, (uint64_t)num_threads * (3ull * ops_per_thread + 128));
+}
+// wf_queue_host_init, wfqueue_hip_opt.hpp:762-764
+static inline cudaError_t wf_queue_host_init(wf_queue** d_q, wf_handle** d_handles, int num_threads) {
+    return wf_queue_host_init_ex(d_q, d_handles, num_threads, WF_PREALLOC_OPS_PER_THREAD);
+}
+// wf_queue_host_init_for_bfs, wfqueue_hip_opt.hpp:697-760
+static inline cudaError_t wf_queue_host_init_for_bfs(wf_queue** d_q, wf_handle** d_handles, int num_threads,
+                                                     long long graph_edges, int graph_vertices, int chunk_size) {
+    if (graph_edges < 0 || graph_vertices < 0 || chunk_size <= 0) return cudaErrorInvalidValue;
+    const uint64_t work_items = ((uint64_t)graph_edges + chunk_size - 1) / chunk_size;
+    const uint64_t cells = (uint64_t)(((uint64_t)graph_vertices + work_items) * 1.20) + 10000;
+    return wf_queue_host_alloc(d_q, d_handles, num_threads, cells);
+}
+// wf_queue_reset_for_bfs, wfqueue_hip_opt.hpp:665-695: clear the used cells, zero
+// T and H, re-initialise the handles.
+static inline cudaError_t wf_queue_reset_for_bfs(wf_queue* d_q, wf_handle* d_handles, int num_threads) {
+    wf_clear_pool_kernel<<<152 * 8, 256>>>(d_q);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemset((void*)&d_q->T, 0, sizeof(d_q->T));
+    if (e == cudaSuccess) e = cudaMemset((void*)&d_q->H, 0, sizeof(d_q->H));
+    if (e != cudaSuccess) return e;
+    const int block = 256;
+    wf_init_kernel<<<(num_threads + block - 1) / block, block>>>(d_q, d_handles, num_threads);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaDeviceSynchronize();
+}
+// Free what the host initialisers allocated (the reference leaves this to hipFree).
+static inline void wf_queue_host_destroy(wf_queue* d_q, wf_handle* d_handles) {
+    if (d_q) cudaFree(d_q);
+    if (d_handles) cudaFree(d_handles);
+}
