@@ -124,7 +124,10 @@ SIGNATURES = {
     "gcq_tb_launch": ([P, I32, I32, U32, U32, U32, U64, P, P], I32),
     "gcq_tb_chunk_host": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
     "gcq_tb_run": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
+    "gcq_tb_run_bounded": ([P, I32, I32, U32, U32, U32, C.c_double, C.c_double, U32, C.POINTER(TbResult)], I32),
     "gcq_fifo_check": ([P, U32, U32, U32, C.POINTER(FifoResult)], I32),
+    "gcq_fifo_check_split": ([P, U32, U32, I32, U32, C.POINTER(FifoResult)], I32),
+    "gcq_drain_host": ([P, U32, U32, P, SZ, C.POINTER(SZ)], I32),
     "gcq_roofline_measure": ([C.POINTER(Roofline), I32], I32),
     "gcq_stats": ([P, C.POINTER(C.c_uint64), I32], I32),
     "gcq_tb_chunk_host_noalloc": ([P, I32, I32, U32, U32, U32, P, C.POINTER(TbCounters), P], I32),
@@ -293,6 +296,19 @@ class Queue:
         r = TbResult()
         _check(_lib().gcq_tb_run(self._h, mode, producer_percent, threads, block, chunk_ops, warmup_ms, run_ms,
                                  graph_chunks, C.byref(r)), "gcq_tb_run")
+        return self._tb_dict(r)
+
+    def tb_run_bounded(self, mode: int, threads: int, chunk_ops: int = 128, block: int = 256,
+                       producer_percent: int = 50, warmup_ms: float = 200.0, run_ms: float = 1000.0,
+                       reset_every: int = 0) -> dict:
+        """gcq_tb_run with a device deadline on every chunk (gcq_tb_run_bounded)."""
+        r = TbResult()
+        _check(_lib().gcq_tb_run_bounded(self._h, mode, producer_percent, threads, block, chunk_ops, warmup_ms,
+                                         run_ms, reset_every, C.byref(r)), "gcq_tb_run_bounded")
+        return self._tb_dict(r)
+
+    @staticmethod
+    def _tb_dict(r) -> dict:
         c = r.counters
         sec = r.gpu_ms / 1e3
         d = {f: getattr(c, f) for f, _ in TbCounters._fields_}
@@ -309,6 +325,21 @@ class Queue:
         r = FifoResult()
         _check(_lib().gcq_fifo_check(self._h, threads, block, ops_per_thread, C.byref(r)), "gcq_fifo_check")
         return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+    def fifo_check_split(self, threads: int, producer_percent: int = 50, ops_per_producer: int = 32,
+                         block: int = 256) -> dict:
+        """Producers and consumers in one launch (gcq_fifo_check_split)."""
+        r = FifoResult()
+        _check(_lib().gcq_fifo_check_split(self._h, threads, block, producer_percent, ops_per_producer,
+                                           C.byref(r)), "gcq_fifo_check_split")
+        return {f: getattr(r, f) for f, _ in FifoResult._fields_ if not f.startswith("_")}
+
+    def drain_host(self, threads: int = 1024, cap: int = 1 << 20, block: int = 256) -> np.ndarray:
+        """Dequeue everything the queue holds into a host array (gcq_drain_host)."""
+        out = np.zeros(cap, dtype=np.uint64)
+        n = SZ()
+        _check(_lib().gcq_drain_host(self._h, threads, block, out.ctypes.data, cap, C.byref(n)), "gcq_drain_host")
+        return out[: n.value].copy()
 
 
 def autotune(kind: str, capacity_log2: int, threads: int, mode: int = 0, producer_percent: int = 50,

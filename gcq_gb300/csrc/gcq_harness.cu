@@ -59,17 +59,22 @@ __device__ __forceinline__ void block_add_counters(uint64_t a, uint64_t b, uint6
 // split_chunk_kernel (mode 1, :842-882) in one body.  Payload i of thread t is
 // payloads[i * threads + t] when payloads is given, else splitmix64(seed, t, i).
 // All lanes stay to the end for the block reduction (the reference returns early).
-template <int K>
+// Bounded: the sweep's form -- every thread stops at the %globaltimer value in
+// *deadline (read once at the start), so one point of a slow configuration cannot
+// run past its window; the counters hold what completed.
+template <int K, bool Bounded = false>
 __global__ void __launch_bounds__(1024) k_tb_chunk(void* qv, int mode, int producer_percent, uint32_t threads,
                                                    uint32_t chunk_ops, uint64_t seed, const uint32_t* payloads,
-                                                   gcq_tb_counters* ctr) {
+                                                   gcq_tb_counters* ctr, const uint64_t* deadline = nullptr) {
     auto* q = as_q<K>(qv);
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t eo = 0, ef = 0, dok = 0, de = 0;
     if (tid < threads) {
         const bool producer = ((uint64_t)tid * 100u / threads) < (uint64_t)producer_percent;
         const bool nb = (mode == 1);   // SFQ: blocking when balanced, non-blocking when split
+        const uint64_t stop = Bounded ? *deadline : 0;
         for (uint32_t i = 0; i < chunk_ops; ++i) {
+            if (Bounded && gcq::globaltimer_ns() > stop) break;
             if (mode == 0 || producer) {
                 const uint32_t p = payloads ? payloads[(uint64_t)i * threads + tid]
                                             : (uint32_t)gcqi::splitmix64(seed ^ (((uint64_t)tid << 32) | i));
@@ -117,6 +122,24 @@ int launch_tb(gcq_queue* q, int mode, int pct, uint32_t threads, uint32_t block,
         case GCQ_GLFQ: k_tb_chunk<GCQ_GLFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
         case GCQ_WFQ: k_tb_chunk<GCQ_WFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
         case GCQ_SFQ: k_tb_chunk<GCQ_SFQ><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, payloads, ctr); break;
+        default: return GCQ_EINVAL;
+    }
+    GCQ_CUDA(cudaGetLastError());
+    return GCQ_OK;
+}
+
+__global__ void k_stamp_deadline(uint64_t* deadline, uint64_t after_ns) {
+    *deadline = gcq::globaltimer_ns() + after_ns;
+}
+
+int launch_tb_bounded(gcq_queue* q, int mode, int pct, uint32_t threads, uint32_t block, uint32_t chunk_ops,
+                      uint64_t seed, gcq_tb_counters* ctr, const uint64_t* deadline, cudaStream_t s) {
+    const unsigned grid = (threads + block - 1) / block;
+    switch (q->kind) {
+        case GCQ_GWFQ: k_tb_chunk<GCQ_GWFQ, true><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, nullptr, ctr, deadline); break;
+        case GCQ_GLFQ: k_tb_chunk<GCQ_GLFQ, true><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, nullptr, ctr, deadline); break;
+        case GCQ_WFQ: k_tb_chunk<GCQ_WFQ, true><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, nullptr, ctr, deadline); break;
+        case GCQ_SFQ: k_tb_chunk<GCQ_SFQ, true><<<grid, block, 0, s>>>(q->obj, mode, pct, threads, chunk_ops, seed, nullptr, ctr, deadline); break;
         default: return GCQ_EINVAL;
     }
     GCQ_CUDA(cudaGetLastError());
@@ -238,6 +261,86 @@ __global__ void k_fifo_drain(void* qv, uint32_t threads, uint32_t ops, uint64_t 
     }
 }
 
+// Concurrent split-mode FIFO check (no counterpart in the reference, whose FIFO
+// mode produces everything before it drains, throughout_bench.cpp:456-767): the
+// threads of the split chunk kernel's producer share (the same thread-to-role rule
+// as k_tb_chunk) each enqueue ops tokens, retrying while the queue is full, while
+// the other threads dequeue them in the same launch until all are consumed.  Every
+// wait has a deadline.  Needs every thread resident (the host checks).
+template <int K>
+__global__ void k_fifo_split(void* qv, uint32_t threads, int pct, uint32_t nprod, uint32_t ops, uint64_t total,
+                             uint32_t* counts,
+                             int64_t* calls, int64_t* ends, gcq::u64a* consumed, gcq::u64a* clock, gcq::u32a* oob,
+                             uint64_t timeout_ns, gcq::u32a* err) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= threads) return;
+    const bool producer = ((uint64_t)tid * 100u / threads) < (uint64_t)pct;
+    if (producer) {
+        for (uint32_t i = 0; i < ops; ++i) {
+            const uint64_t tok = fifo_token(K, tid, i);
+            gcq::backoff bo;
+            const uint64_t t0 = gcq::globaltimer_ns();
+            while (!qops<K>::enq(q, tok, tid, true)) {
+                if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+                bo.pause(512);
+            }
+        }
+        return;
+    }
+    gcq::backoff bo;
+    uint64_t t0 = gcq::globaltimer_ns();
+    while (gcq::ld_acq(consumed) < total) {
+        const int64_t c0 = (int64_t)gcq::fetch_add(clock, 1ull);
+        uint64_t v = 0;
+        const int r = qops<K>::deq(q, &v, tid, true);
+        const int64_t c1 = (int64_t)gcq::fetch_add(clock, 1ull);
+        if (r != 1) {
+            if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+            bo.pause(512);
+            continue;
+        }
+        bo = gcq::backoff();
+        t0 = gcq::globaltimer_ns();
+        if (gcq::fetch_add(consumed, 1ull) >= total) continue;
+        uint32_t ptid, seq;
+        if (K == GCQ_SFQ) { ptid = (uint32_t)(v >> 16) & 0x7FFFu; seq = ((uint32_t)v & 0xFFFFu) - 1u; }
+        else { ptid = (uint32_t)(v >> 32); seq = (uint32_t)v - 1u; }
+        // counts/calls/ends hold nprod * ops slots: producers are threads 0..nprod-1
+        if (ptid >= nprod || seq >= ops) { atomicAdd(oob, 1u); continue; }
+        const uint64_t slot = (uint64_t)ptid * ops + seq;
+        if (atomicAdd(&counts[slot], 1u) == 0u) {
+            calls[slot] = c0;
+            ends[slot] = c1;
+        }
+    }
+}
+
+// Drain a quiescent queue into out[0 .. cap): each thread dequeues until its
+// dequeue reports empty (SFQ's non-blocking dequeue cannot tell empty from a lost
+// race, so there a run of failed attempts ends the thread).
+template <int K>
+__global__ void k_drain(void* qv, uint32_t threads, uint64_t* out, uint64_t cap, gcq::u64a* n) {
+    auto* q = as_q<K>(qv);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= threads) return;
+    uint32_t fails = 0;
+    gcq::backoff bo;
+    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k) {
+        uint64_t v = 0;
+        const int r = qops<K>::deq(q, &v, tid, true);
+        if (r == 0) return;
+        if (r == 2) {
+            if (++fails > 256) return;
+            bo.pause(1024);
+            continue;
+        }
+        fails = 0;
+        const uint64_t i = gcq::fetch_add(n, 1ull);
+        if (i < cap) out[i] = v;
+    }
+}
+
 template <typename F>
 int dispatch(int kind, F&& f) {
     switch (kind) {
@@ -309,8 +412,10 @@ int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t thr
     rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, direct ? direct : d_pay, d_ctr, s);
     if (rc != GCQ_OK) return rc;
     GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
-    GCQ_CUDA(cudaStreamSynchronize(s));
-    return GCQ_OK;
+    uint32_t err = 0;
+    rc = read_error_word(q, s, &err);   // synchronises s
+    if (rc != GCQ_OK) return rc;
+    return status_of(err);
 }
 
 int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
@@ -375,6 +480,69 @@ int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, u
     return status_of(err);
 }
 
+int gcq_tb_run_bounded(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                       uint32_t chunk_ops, double warmup_ms, double run_ms, uint32_t reset_every,
+                       gcq_tb_result* out) {
+    int rc = check_tb_args(q, mode, producer_percent, threads, block, chunk_ops);
+    if (rc != GCQ_OK) return rc;
+    if (!out || warmup_ms < 0 || run_ms <= 0) return GCQ_EINVAL;
+    memset(out, 0, sizeof(*out));
+    cudaStream_t s;
+    GCQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    dbuf buf;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaStreamDestroy(s);
+    };
+    auto fail = [&](int r) { cleanup(); return r; };
+    if (buf.alloc(256) != cudaSuccess) return fail(GCQ_ENOMEM);
+    gcq_tb_counters* d_ctr = (gcq_tb_counters*)buf.p;
+    uint64_t* d_deadline = (uint64_t*)((char*)buf.p + 128);
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return fail(GCQ_ECUDA);
+    using clk = std::chrono::steady_clock;
+    uint64_t chunks = 0, seed = 0x5eedULL;
+    double ms = 0.0;
+    // one window: the device deadline is stamped at its start, then chunks run until
+    // host time passes the window (each chunk also stops at the device deadline)
+    auto window = [&](double win_ms, bool timed) -> int {
+        if (cudaMemsetAsync(d_ctr, 0, sizeof(gcq_tb_counters), s) != cudaSuccess) return GCQ_ECUDA;
+        k_stamp_deadline<<<1, 1, 0, s>>>(d_deadline, (uint64_t)(win_ms * 1e6));
+        const auto t0 = clk::now();
+        do {
+            if (reset_every && chunks % reset_every == 0) {
+                const int r = gcq_reset(q, s);
+                if (r != GCQ_OK) return r;
+            }
+            if (timed && cudaEventRecord(e0, s) != cudaSuccess) return GCQ_ECUDA;
+            const int r = launch_tb_bounded(q, mode, producer_percent, threads, block, chunk_ops, seed++, d_ctr,
+                                            d_deadline, s);
+            if (r != GCQ_OK) return r;
+            if (timed && cudaEventRecord(e1, s) != cudaSuccess) return GCQ_ECUDA;
+            if (cudaStreamSynchronize(s) != cudaSuccess) return GCQ_ECUDA;
+            ++chunks;
+            if (timed) {
+                float m = 0.f;
+                cudaEventElapsedTime(&m, e0, e1);
+                ms += m;
+                ++out->launches;
+            }
+        } while (std::chrono::duration<double, std::milli>(clk::now() - t0).count() < win_ms);
+        return GCQ_OK;
+    };
+    if (warmup_ms > 0 && (rc = window(warmup_ms, false)) != GCQ_OK) return fail(rc);
+    if ((rc = window(run_ms, true)) != GCQ_OK) return fail(rc);
+    if (cudaMemcpy(&out->counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(GCQ_ECUDA);
+    out->gpu_ms = ms;
+    uint32_t err = 0;
+    rc = read_error_word(q, s, &err);
+    cleanup();
+    if (rc != GCQ_OK) return rc;
+    return status_of(err);
+}
+
 int gcq_run_history(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops, int mode,
                     int producer_percent, int value_mode, gcq_log_entry* host_out, size_t cap,
                     size_t* n_out, void* stream) {
@@ -422,6 +590,69 @@ int gcq_run_history(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops
     return status_of(err);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device buffers of one FIFO check and the host-side verdict: exactly once (in and
+// out counts, duplicates, missing, out of range) and per-producer order -- for
+// tokens a < b of one producer, the dequeue of b must not return before the
+// dequeue of a was called (logical clock).  The reference's order check
+// (throughout_bench.cpp:585-588) starts its atomicMax from 0xFFFFFFFF (:691) and
+// never fires.
+struct fifo_bufs {
+    dbuf counts, calls, ends, misc;
+    gcq::u64a* consumed() { return (gcq::u64a*)misc.p; }
+    gcq::u64a* clock() { return (gcq::u64a*)misc.p + 1; }
+    gcq::u32a* oob() { return (gcq::u32a*)((gcq::u64a*)misc.p + 2); }
+    int alloc(uint64_t total) {
+        if (counts.alloc(total * 4) != cudaSuccess || calls.alloc(total * 8) != cudaSuccess ||
+            ends.alloc(total * 8) != cudaSuccess || misc.alloc(256) != cudaSuccess)
+            return GCQ_ENOMEM;
+        GCQ_CUDA(cudaMemset(counts.p, 0, total * 4));
+        GCQ_CUDA(cudaMemset(misc.p, 0, 256));
+        const unsigned long long one = 1;
+        GCQ_CUDA(cudaMemcpy(clock(), &one, 8, cudaMemcpyHostToDevice));
+        return GCQ_OK;
+    }
+};
+
+// producers: thread indices p with slots p*ops .. p*ops+ops-1
+int fifo_verify(gcq_queue* q, fifo_bufs& b, const std::vector<uint32_t>& producers, uint64_t ops, uint64_t total,
+                gcq_fifo_result* out) {
+    GCQ_CUDA(cudaGetLastError());
+    GCQ_CUDA(cudaDeviceSynchronize());
+    const uint64_t nslots = (uint64_t)(producers.empty() ? 0 : producers.back() + 1) * ops;
+    std::vector<uint32_t> hc(nslots);
+    std::vector<int64_t> hcall(nslots), hend(nslots);
+    uint64_t hmisc[4];
+    GCQ_CUDA(cudaMemcpy(hc.data(), b.counts.p, nslots * 4, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hcall.data(), b.calls.p, nslots * 8, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hend.data(), b.ends.p, nslots * 8, cudaMemcpyDeviceToHost));
+    GCQ_CUDA(cudaMemcpy(hmisc, b.misc.p, sizeof hmisc, cudaMemcpyDeviceToHost));
+    out->out_count = std::min<uint64_t>(hmisc[0], total);
+    out->err_oob = (uint32_t)hmisc[2];
+    for (uint32_t p : producers) {
+        int64_t max_call = -1;
+        for (uint64_t sq = 0; sq < ops; ++sq) {
+            const uint64_t slot = (uint64_t)p * ops + sq;
+            if (hc[slot] == 0) { out->err_missing++; continue; }
+            if (hc[slot] > 1) { out->err_gt1++; out->err_dup += hc[slot] - 1; }
+            if (hend[slot] < max_call) out->err_order++;
+            max_call = std::max(max_call, hcall[slot]);
+        }
+    }
+    uint32_t err = 0;
+    GCQ_CUDA(cudaMemcpy(&err, q->err, 4, cudaMemcpyDeviceToHost));
+    out->verified = (out->out_count == out->in_count && !out->err_oob && !out->err_dup && !out->err_order &&
+                     !out->err_missing && !out->err_gt1) ? 1 : 0;
+    return status_of(err);
+}
+
+}  // namespace
+
+extern "C" {
+
 int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
                    gcq_fifo_result* out) {
     if (!q || !out || threads == 0 || block == 0 || block > 1024) return GCQ_EINVAL;
@@ -444,52 +675,96 @@ int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_
     out->in_count = total;
     int rc = gcq_reset(q, nullptr);
     if (rc != GCQ_OK) return rc;
-    dbuf counts, calls, ends, misc;
-    if (counts.alloc(total * 4) != cudaSuccess || calls.alloc(total * 8) != cudaSuccess ||
-        ends.alloc(total * 8) != cudaSuccess || misc.alloc(256) != cudaSuccess)
-        return GCQ_ENOMEM;
-    GCQ_CUDA(cudaMemset(counts.p, 0, total * 4));
-    GCQ_CUDA(cudaMemset(misc.p, 0, 256));
-    gcq::u64a* consumed = (gcq::u64a*)misc.p;
-    gcq::u64a* clock = consumed + 1;
-    gcq::u32a* oob = (gcq::u32a*)(consumed + 2);
-    const unsigned long long one = 1;
-    GCQ_CUDA(cudaMemcpy(clock, &one, 8, cudaMemcpyHostToDevice));
+    fifo_bufs b;
+    rc = b.alloc(total);
+    if (rc != GCQ_OK) return rc;
     const unsigned grid = (threads + block - 1) / block;
     const uint64_t tmo = std::max<uint64_t>(q->knobs.wait_timeout_ns, 1000000000ull) * 4;
     rc = dispatch(q->kind, [&](auto kc) {
         constexpr int K = decltype(kc)::value;
         k_fifo_produce<K><<<grid, block>>>(q->obj, threads, (uint32_t)ops, tmo, q->err);
-        k_fifo_drain<K><<<grid, block>>>(q->obj, threads, (uint32_t)ops, total, (uint32_t*)counts.p,
-                                         (int64_t*)calls.p, (int64_t*)ends.p, consumed, clock, oob, tmo, q->err);
+        k_fifo_drain<K><<<grid, block>>>(q->obj, threads, (uint32_t)ops, total, (uint32_t*)b.counts.p,
+                                         (int64_t*)b.calls.p, (int64_t*)b.ends.p, b.consumed(), b.clock(), b.oob(),
+                                         tmo, q->err);
         return GCQ_OK;
     });
+    std::vector<uint32_t> producers(threads);
+    for (uint32_t p = 0; p < threads; ++p) producers[p] = p;
+    return fifo_verify(q, b, producers, ops, total, out);
+}
+
+int gcq_drain_host(gcq_queue* q, uint32_t threads, uint32_t block, uint64_t* host_out, size_t cap,
+                   size_t* n_out) {
+    if (!q || !n_out || (cap && !host_out) || threads == 0 || block == 0 || block > 1024 || (block & 31))
+        return GCQ_EINVAL;
+    if (threads > q->max_threads) return GCQ_EINVAL;
+    dbuf buf, cnt;
+    if ((cap && buf.alloc(cap * 8) != cudaSuccess) || cnt.alloc(256) != cudaSuccess) return GCQ_ENOMEM;
+    GCQ_CUDA(cudaMemset(cnt.p, 0, 256));
+    const unsigned grid = (threads + block - 1) / block;
+    int rc = dispatch(q->kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_drain<K><<<grid, block>>>(q->obj, threads, (uint64_t*)buf.p, (uint64_t)cap, (gcq::u64a*)cnt.p);
+        return GCQ_OK;
+    });
+    if (rc != GCQ_OK) return rc;
     GCQ_CUDA(cudaGetLastError());
     GCQ_CUDA(cudaDeviceSynchronize());
-    std::vector<uint32_t> hc(total);
-    std::vector<int64_t> hcall(total), hend(total);
-    uint64_t hmisc[4];
-    GCQ_CUDA(cudaMemcpy(hc.data(), counts.p, total * 4, cudaMemcpyDeviceToHost));
-    GCQ_CUDA(cudaMemcpy(hcall.data(), calls.p, total * 8, cudaMemcpyDeviceToHost));
-    GCQ_CUDA(cudaMemcpy(hend.data(), ends.p, total * 8, cudaMemcpyDeviceToHost));
-    GCQ_CUDA(cudaMemcpy(hmisc, misc.p, sizeof hmisc, cudaMemcpyDeviceToHost));
-    out->out_count = std::min<uint64_t>(hmisc[0], total);
-    out->err_oob = (uint32_t)hmisc[2];
-    for (uint32_t p = 0; p < threads; ++p) {
-        int64_t max_call = -1;
-        for (uint64_t sq = 0; sq < ops; ++sq) {
-            const uint64_t slot = (uint64_t)p * ops + sq;
-            if (hc[slot] == 0) { out->err_missing++; continue; }
-            if (hc[slot] > 1) { out->err_gt1++; out->err_dup += hc[slot] - 1; }
-            if (hend[slot] < max_call) out->err_order++;
-            max_call = std::max(max_call, hcall[slot]);
-        }
-    }
+    uint64_t n = 0;
+    GCQ_CUDA(cudaMemcpy(&n, cnt.p, 8, cudaMemcpyDeviceToHost));
+    const uint64_t keep = std::min<uint64_t>(n, cap);
+    if (keep) GCQ_CUDA(cudaMemcpy(host_out, buf.p, keep * 8, cudaMemcpyDeviceToHost));
+    *n_out = (size_t)keep;
     uint32_t err = 0;
     GCQ_CUDA(cudaMemcpy(&err, q->err, 4, cudaMemcpyDeviceToHost));
-    out->verified = (out->out_count == out->in_count && !out->err_oob && !out->err_dup && !out->err_order &&
-                     !out->err_missing && !out->err_gt1) ? 1 : 0;
+    if (n > cap) return GCQ_ECAPACITY;
     return status_of(err);
+}
+
+int gcq_fifo_check_split(gcq_queue* q, uint32_t threads, uint32_t block, int producer_percent,
+                         uint32_t ops_per_producer, gcq_fifo_result* out) {
+    if (!q || !out || threads == 0 || block == 0 || block > 1024 || (block & 31) || ops_per_producer == 0)
+        return GCQ_EINVAL;
+    if (producer_percent <= 0 || producer_percent >= 100) return GCQ_EINVAL;
+    if (threads > q->max_threads) return GCQ_EINVAL;
+    memset(out, 0, sizeof(*out));
+    uint64_t ops = ops_per_producer;
+    if (q->kind == GCQ_SFQ) {
+        if (threads > 32768u) return GCQ_EUNSUPPORTED;   // 15-bit producer field of the token
+        ops = std::min<uint64_t>(ops, 0xFFFFu);
+    }
+    // producers wait for consumers and consumers for producers: all must be resident
+    uint64_t res = 0;
+    int rc = dispatch(q->kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        return gcqi::resident_threads((const void*)k_fifo_split<K>, (int)block, 0, &res);
+    });
+    if (rc != GCQ_OK) return rc;
+    if (threads > res) return GCQ_EUNSUPPORTED;
+    std::vector<uint32_t> producers;
+    for (uint32_t t = 0; t < threads; ++t)
+        if ((uint64_t)t * 100u / threads < (uint64_t)producer_percent) producers.push_back(t);
+    if (producers.empty() || producers.size() == threads || producers.back() + 1 != producers.size())
+        return GCQ_EINVAL;
+    const uint64_t total = (uint64_t)producers.size() * ops;
+    out->ops_per_thread = (uint32_t)ops;
+    out->in_count = total;
+    rc = gcq_reset(q, nullptr);
+    if (rc != GCQ_OK) return rc;
+    fifo_bufs b;
+    rc = b.alloc((uint64_t)(producers.back() + 1) * ops);
+    if (rc != GCQ_OK) return rc;
+    const unsigned grid = (threads + block - 1) / block;
+    const uint64_t tmo = std::max<uint64_t>(q->knobs.wait_timeout_ns, 1000000000ull) * 4;
+    rc = dispatch(q->kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_fifo_split<K><<<grid, block>>>(q->obj, threads, producer_percent, (uint32_t)producers.size(),
+                                         (uint32_t)ops, total,
+                                         (uint32_t*)b.counts.p, (int64_t*)b.calls.p, (int64_t*)b.ends.p,
+                                         b.consumed(), b.clock(), b.oob(), tmo, q->err);
+        return GCQ_OK;
+    });
+    return fifo_verify(q, b, producers, ops, total, out);
 }
 
 }  // extern "C"
@@ -507,25 +782,54 @@ constexpr uint64_t kNoallocPayloadWords = GCQ_NOALLOC_MAX_PAYLOADS;
 constexpr uint64_t kNoallocWords = kNoallocPayloadWords + 64;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoallocWords];
 
-// Device address of g_noalloc_scratch, looked up once per device.  In host code the
-// array's name stands for a host-side shadow, not a device address, so it must never
-// be passed to a kernel; cudaGetSymbolAddress gives the address on the current device.
-constexpr int kMaxDevices = 64;
+// Device address of g_noalloc_scratch, looked up once per CUDA context.  In host
+// code the array's name stands for a host-side shadow, not a device address, so it
+// must never be passed to a kernel; cudaGetSymbolAddress gives the address in the
+// current device's context.  The cache is keyed by the context's unique id
+// (cuCtxGetId, reached through the runtime's driver entry points, so the library
+// does not link libcuda): after cudaDeviceReset the device's new primary context
+// has a new id, and the first call in it looks the address up again.
+typedef int (*ctx_get_current_fn)(void** ctx);
+typedef int (*ctx_get_id_fn)(void* ctx, unsigned long long* id);
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {};
+ctx_get_current_fn g_ctx_get_current = nullptr;
+ctx_get_id_fn g_ctx_get_id = nullptr;
+std::map<unsigned long long, void*> g_noalloc_ptr;   // context id -> device address
+
+int current_ctx_id(unsigned long long* id) {
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx) return GCQ_ECUDA;
+    if (g_ctx_get_id(ctx, id) != 0) return GCQ_ECUDA;
+    return GCQ_OK;
+}
 
 int noalloc_scratch(void** out) {
-    int dev = 0;
-    GCQ_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return GCQ_EUNSUPPORTED;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        GCQ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        if (!p) return GCQ_ECUDA;
-        g_noalloc_ptr[dev] = p;
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult r1, r2;
+        void *f1 = nullptr, *f2 = nullptr;
+        GCQ_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &r1));
+        GCQ_CUDA(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &r2));
+        if (r1 != cudaDriverEntryPointSuccess || r2 != cudaDriverEntryPointSuccess || !f1 || !f2) return GCQ_ECUDA;
+        g_ctx_get_current = (ctx_get_current_fn)f1;
+        g_ctx_get_id = (ctx_get_id_fn)f2;
     }
-    *out = g_noalloc_ptr[dev];
+    unsigned long long id = 0;
+    if (current_ctx_id(&id) == GCQ_OK) {
+        auto it = g_noalloc_ptr.find(id);
+        if (it != g_noalloc_ptr.end()) {
+            *out = it->second;
+            return GCQ_OK;
+        }
+    }
+    // set-up in this context (it also makes the device's primary context current
+    // when no runtime call has done so in this thread yet)
+    void* p = nullptr;
+    GCQ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    if (!p) return GCQ_ECUDA;
+    if (current_ctx_id(&id) != GCQ_OK) return GCQ_ECUDA;
+    g_noalloc_ptr[id] = p;
+    *out = p;
     return GCQ_OK;
 }
 
@@ -551,8 +855,10 @@ extern "C" int gcq_tb_chunk_host_noalloc(gcq_queue* q, int mode, int producer_pe
     rc = launch_tb(q, mode, producer_percent, threads, block, chunk_ops, 0, d_pay, d_ctr, s);
     if (rc != GCQ_OK) return rc;
     GCQ_CUDA(cudaMemcpyAsync(host_counters, d_ctr, sizeof(gcq_tb_counters), cudaMemcpyDeviceToHost, s));
-    GCQ_CUDA(cudaStreamSynchronize(s));
-    return GCQ_OK;
+    uint32_t err = 0;
+    rc = read_error_word(q, s, &err);   // synchronises s
+    if (rc != GCQ_OK) return rc;
+    return status_of(err);
 }
 
 // ------------------------------------------------------------------ autotuner

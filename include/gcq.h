@@ -157,7 +157,10 @@ int gcq_tb_launch(gcq_queue* q, int mode, int producer_percent, uint32_t threads
  * (payload i of thread t at host_payloads[i * threads + t]) to the GPU, runs one
  * chunk with them, and copies the counters of that chunk back to host_counters.
  * Pinned payloads (cudaHostAlloc / cudaHostRegister) are read by the kernel in
- * place over the host link while it runs; pageable ones are copied first. */
+ * place over the host link while it runs; pageable ones are copied first.  The
+ * call synchronises `stream`, then reads the queue's error word: GCQ_ETIMEDOUT or
+ * GCQ_EDEVICE when a bounded wait or retry loop gave up during the chunk (the
+ * counters then hold what completed), as gcq_tb_run does. */
 int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
                       uint32_t chunk_ops, const uint32_t* host_payloads, gcq_tb_counters* host_counters,
                       void* stream);
@@ -172,12 +175,14 @@ int gcq_tb_chunk_host(gcq_queue* q, int mode, int producer_percent, uint32_t thr
  * memory.  The payload staging and the counters live in a fixed 16 MiB + 256 B
  * array compiled into libgcq.so (GCQ_NOALLOC_MAX_PAYLOADS payloads; larger
  * threads * chunk_ops returns GCQ_ECAPACITY).  Every GPU that loads the library
- * holds that array until the process exits.  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) and caches it; make that first
- * call before any stream capture.  All calls share the one array: the counters are
- * cleared at the start of every call, and calls whose work overlaps on the GPU (on
- * different streams, or from different host threads) race on it.  Arguments and
- * results are those of gcq_tb_chunk_host. */
+ * holds that array until the process exits.  The first call in each CUDA context
+ * (per device, and again after cudaDeviceReset) looks up the array's device
+ * address with cudaGetSymbolAddress and caches it by the context's id; make that
+ * first call before any stream capture.  Like gcq_tb_chunk_host, every call
+ * synchronises `stream` before it returns.  All calls share the one array: the
+ * counters are cleared at the start of every call, and calls whose work overlaps
+ * on the GPU (on different streams, or from different host threads) race on it.
+ * Arguments, results and error returns are those of gcq_tb_chunk_host. */
 int gcq_tb_chunk_host_noalloc(gcq_queue* q, int mode, int producer_percent, uint32_t threads,
                               uint32_t block, uint32_t chunk_ops, const uint32_t* host_payloads,
                               gcq_tb_counters* host_counters, void* stream);
@@ -195,6 +200,21 @@ typedef struct gcq_tb_result {
 int gcq_tb_run(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
                uint32_t chunk_ops, double warmup_ms, double run_ms, uint32_t graph_chunks,
                gcq_tb_result* out);
+
+/* Fixed-duration run for sweeps: gcq_tb_run with every chunk kernel bounded by a
+ * device deadline (%globaltimer), stamped at the start of the warm-up and of the
+ * timed window, so a configuration whose chunk would run for seconds (SFQ's
+ * non-blocking split mode, many consumers polling an almost empty queue) ends with
+ * its window and reports the operations it completed.  Chunks are launched one at
+ * a time; gpu_ms sums their CUDA-event times.  reset_every > 0 re-initialises the
+ * queue (gcq_reset, outside the timed events) before every reset_every-th chunk:
+ * YMC consumes its cell pool without reclamation (wfqueue_hip_opt.hpp:208-237), so
+ * a reset gives each chunk a fresh pool.  0 never resets.  The reference's loop
+ * (run_balanced_timed / run_split_timed, throughout_bench.cpp:959-1051) has no
+ * bound on a chunk. */
+int gcq_tb_run_bounded(gcq_queue* q, int mode, int producer_percent, uint32_t threads, uint32_t block,
+                       uint32_t chunk_ops, double warmup_ms, double run_ms, uint32_t reset_every,
+                       gcq_tb_result* out);
 
 /* ------------------------------------------------------------- FIFO check ----
  * Produce-then-drain check of throughout_bench.cpp:456-767 (MODE_FIFO).  Every
@@ -233,6 +253,28 @@ typedef struct gcq_fifo_result {
 
 int gcq_fifo_check(gcq_queue* q, uint32_t threads, uint32_t block, uint32_t ops_per_thread,
                    gcq_fifo_result* out);
+
+/* The same exactly-once and per-producer order check with producers and consumers
+ * running at once, in the roles of split_chunk_kernel (throughout_bench.cpp:842-882:
+ * thread t produces when t * 100 / threads < producer_percent).  Each producer
+ * enqueues ops_per_producer tokens, retrying while the queue is full; the others
+ * dequeue until every token is taken.  No counterpart in the reference, whose FIFO
+ * mode produces everything before it drains.  Producers and consumers wait for one
+ * another, so every thread must be resident at once: more threads than the device
+ * holds returns GCQ_EUNSUPPORTED (as does SFQ above 32768 threads, its token's
+ * producer field).  producer_percent in 1..99.  The queue is reset first. */
+int gcq_fifo_check_split(gcq_queue* q, uint32_t threads, uint32_t block, int producer_percent,
+                         uint32_t ops_per_producer, gcq_fifo_result* out);
+
+/* Dequeue everything the queue holds into host_out (at most cap values) with
+ * `threads` threads of the per-thread API, stopping when each thread's dequeue
+ * reports empty; *n_out receives the count.  Meant for a quiescent queue (no
+ * operation in flight): then an empty dequeue means empty.  Values are returned as
+ * the queue holds them (YMC: payload + 1; SFQ: the 32-bit item).  GCQ_ECAPACITY
+ * when more than cap values come out (the first cap are kept).  No counterpart in
+ * the reference; the tests use it to check a queue's contents. */
+int gcq_drain_host(gcq_queue* q, uint32_t threads, uint32_t block, uint64_t* host_out, size_t cap,
+                   size_t* n_out);
 
 /* ------------------------------------------------------------------ BFS ----
  * Level-synchronous BFS with a queue as the frontier (concurrent_bfs/bfs_bench.cpp). */

@@ -40,6 +40,30 @@ def test_noalloc_matches_chunk_host_twice(gcq):
         assert q.error_word() == 0
 
 
+def test_noalloc_payloads_reach_the_queue_twice(gcq):
+    """The payloads themselves, not only the counts: with every thread a producer
+    (split mode, 100 %), a call enqueues all its payloads, and a drain returns
+    exactly that multiset -- from gcq_tb_chunk_host and from the no-allocation entry
+    point alike, on two calls in a row with different payloads (the second call
+    stages over what the first one left in the shared array)."""
+    threads, chunk = 4096, 16
+    rng = np.random.default_rng(13)
+    for rep in range(2):
+        pay = rng.integers(0, 2**32, size=threads * chunk, dtype=np.uint64).astype(np.uint32)
+        want = np.sort(pay.astype(np.uint64))
+        with gcq.Queue("gwfq", 16, threads) as q:
+            c = q.tb_chunk_host(1, threads, chunk, pay, producer_percent=100)
+            assert c["enq_success"] == threads * chunk
+            ref = np.sort(q.drain_host(threads=1024, cap=1 << 17))
+        with gcq.Queue("gwfq", 16, threads) as q:
+            c = q.tb_chunk_host_noalloc(1, threads, chunk, pay, producer_percent=100)
+            assert c["enq_success"] == threads * chunk
+            got = np.sort(q.drain_host(threads=1024, cap=1 << 17))
+            assert q.error_word() == 0
+        assert np.array_equal(ref, want)
+        assert np.array_equal(got, want)
+
+
 def test_noalloc_rejects_oversize(gcq):
     threads, chunk = 65536, 128   # 8 Mi payloads > 4 Mi maximum
     pay = np.zeros(threads * chunk, dtype=np.uint32)
