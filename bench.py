@@ -371,11 +371,23 @@ def run_gpu(args):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        cc = q.tb_chunk_host(0, threads, chunk, pay, block=BLOCK, stream=sptr)
+        cc = q.tb_chunk_host(0, threads, chunk, pay, block=BLOCK, stream=sptr)   # raises on a device error
         e2e_s += time.perf_counter() - t0
         e2e_ops += cc["enq_success"] + cc["deq_success"]
+        # balanced, capacity >= threads: every enqueue and every dequeue succeeds
+        if not (cc["enq_success"] == cc["deq_success"] == threads * chunk):
+            raise RuntimeError("end-to-end chunk %d counted %s, not %d operations each" % (i, cc, threads * chunk))
+    err = q.error_word()
+    if err & ~g.ERR_POOL:
+        raise RuntimeError("queue error word 0x%x after the end-to-end chunks" % err)
     e2e_s, e2e_ops = whole_job(e2e_s, e2e_ops, device=dev)
     e2e = e2e_ops / (e2e_s * 1e6)
+
+    # ---- the timed queue's values: produce-then-drain FIFO check at the same size
+    # (the reference's FIFO mode; ops per thread capped to capacity / threads)
+    fifo = q.fifo_check(threads=threads, ops_per_thread=32, block=BLOCK)
+    if fifo["verified"] != 1:
+        raise RuntimeError("FIFO check of the bench queue failed: %s" % fifo)
 
     if rank == 0:
         per_launch_ms = dev_ms / args.steps
@@ -392,7 +404,9 @@ def run_gpu(args):
             "peak_source": "measured in this run by gcq_roofline_measure: max of spread 64-bit "
                            "fetch-add on distinct lines (%.1f G/s) and warp-contiguous words (%.1f G/s)"
                            % (peaks["rs_lines"] / 1e9, peaks["rs_contig"] / 1e9),
-            "ticket_ceiling_mops": round(peaks["r1_warp"] / 4 / 1e6, 1),
+            # 4 ticket counters (fq.Head, aq.Tail, aq.Head, fq.Tail), each at most the
+            # measured single-word ticket rate; a successful operation takes 2 tickets
+            "ticket_ceiling_mops": round(4 * peaks["r1_warp"] / 2 / 1e6, 1),
             "single_address_gatomic_s": round(peaks["r1_single"] / 1e9, 3),
             "hbm_measured_gbs": round(peaks["hbm_gbs"], 1),
         }
@@ -418,16 +432,161 @@ def run_gpu(args):
             "step_ms": {"min": round(min(step_ms), 4), "median": round(statistics.median(step_ms), 4),
                         "max": round(max(step_ms), 4)},
             "counters": {"enq_success": c[0], "enq_fail": c[1], "deq_success": c[2], "deq_empty": c[3]},
+            "fifo_verified": fifo["verified"],
+            "fifo": {"threads": threads, "capacity_log2": args.capacity_log2,
+                     "ops_per_thread": fifo["ops_per_thread"], "in": fifo["in_count"], "out": fifo["out_count"],
+                     "check": "produce-then-drain of the timed queue: exactly once, per-producer order"},
         }
         if not args.no_per_queue:
             line["queues"] = per_queue(g)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+        if not args.tb_only:
+            line.update(other_workloads(args, local))
         print(json.dumps(line), flush=True)
     q.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+SWEEP_METRIC = "queue succ Mops/s sweep (4 queues x capacity 2^15/2^20 x balanced/split 50/split 25 x 2^10..2^18 threads)"
+SWEEP_MODES = (("balanced", 0, 50), ("split50", 1, 50), ("split25", 1, 25))
+FIFO_NAMES = {1: "YES", 0: "NO", -1: "skipped"}
+
+
+def sweep_points(kinds, caps, threads_list):
+    """(kind, capacity_log2, mode name, mode, producer percent, threads) of the sweep.
+    YMC has no capacity (its cell pool grows with the thread count), so it is swept
+    once, with capacity_log2 None."""
+    for kind in kinds:
+        for cap in ((None,) if kind == "wfq" else caps):
+            for name, mode, pct in SWEEP_MODES:
+                for t in threads_list:
+                    yield kind, cap, name, mode, pct, t
+
+
+def run_sweep(args):
+    """The throughput sweep: every queue x capacity x mode x thread count, each point
+    a bounded fixed-duration run (gcq_tb_run_bounded: 128-op chunks, warm-up, timed
+    window, every chunk stopped at a device deadline) followed by the reference's
+    FIFO check at 32 ops per producer (capped to capacity / threads; "skipped" when
+    that is 0, as throughout_bench.cpp:633-635 reports it)."""
+    import gcq_gb300 as g
+    rank, world, local = _env_rank()
+    if rank != 0:
+        return 0   # replicas only: the sweep runs on one GPU
+    kinds = args.sweep_queues.split(",")
+    threads_list = [1 << k for k in range(args.sweep_min_log2, args.sweep_max_log2 + 1)]
+    rows, t0 = [], time.perf_counter()
+    sampler = ClockSampler(local)
+    sampler.start()
+    for kind, cap, name, mode, pct, t in sweep_points(kinds, (15, 20), threads_list):
+        row = {"queue": kind, "capacity_log2": cap, "mode": name, "threads": t}
+        try:
+            q = g.Queue(kind, cap or 0, t)
+        except g.GcqError as e:
+            row["status"] = "n/a: %s" % e
+            rows.append(row)
+            continue
+        try:
+            r = q.tb_run_bounded(mode, t, chunk_ops=128, producer_percent=pct, warmup_ms=args.sweep_warmup_ms,
+                                 run_ms=args.sweep_run_ms, reset_every=1 if kind == "wfq" else 0)
+            row.update(status="ok", succ_mops=round(r["succ_mops"], 2), enq_mops=round(r["enq_mops"], 2),
+                       deq_mops=round(r["deq_mops"], 2), launches=r["launches"], gpu_ms=round(r["gpu_ms"], 1))
+            f = q.fifo_check(threads=t, ops_per_thread=32)
+            row["fifo"] = FIFO_NAMES[f["verified"]]
+            row["fifo_ops"] = f["ops_per_thread"]
+        except g.GcqError as e:
+            row["status"] = ("n/a: %s" % e) if e.status == g.EUNSUPPORTED else ("error: %s" % e)
+        finally:
+            q.close()
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+    clocks = sampler.stop()
+    bad = [r for r in rows if r.get("fifo") == "NO" or r["status"].startswith("error")]
+    if args.sweep_md:
+        with open(args.sweep_md, "w") as f:
+            f.write(sweep_markdown(rows, args))
+    head = [r for r in rows if (r["queue"], r["capacity_log2"], r["mode"], r["threads"]) ==
+            ("gwfq", 20, "balanced", threads_list[-1]) and r["status"] == "ok"]
+    line = {
+        "metric": SWEEP_METRIC, "value": head[0]["succ_mops"] if head else None, "unit": "Mops/s",
+        "n_gpus": 1, "steps": len(rows), "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (uint32 payloads from a seed)",
+        "config": {"workload": "throughput sweep: %s x capacity 2^15, 2^20 (YMC: pool) x balanced, split 50 %%, "
+                               "split 25 %% x 2^%d..2^%d threads, block 256, 128 ops per chunk, %.0f ms warm-up, "
+                               "%.0f ms timed; FIFO check at 32 ops per producer"
+                               % ("/".join(kinds), args.sweep_min_log2, args.sweep_max_log2,
+                                  args.sweep_warmup_ms, args.sweep_run_ms),
+                   "value": "G-WFQ balanced, capacity 2^20, 2^%d threads" % args.sweep_max_log2},
+        "points": len(rows), "measured": sum(1 for r in rows if r["status"] == "ok"),
+        "not_applicable": sum(1 for r in rows if r["status"].startswith("n/a")),
+        "failures": len(bad), "wall_s": round(time.perf_counter() - t0, 1), "clocks": clocks,
+        "gpu_launches": sum(r.get("launches", 0) for r in rows),
+        "table": rows,
+    }
+    print(json.dumps(line), flush=True)
+    return 1 if bad else 0
+
+
+def sweep_markdown(rows, args):
+    out = ["| queue | capacity | mode | " + " | ".join("2^%d" % k for k in range(args.sweep_min_log2,
+                                                                           args.sweep_max_log2 + 1)) + " |",
+           "|---|---|---|" + "---:|" * (args.sweep_max_log2 - args.sweep_min_log2 + 1)]
+    keyed = {}
+    for r in rows:
+        keyed.setdefault((r["queue"], r["capacity_log2"], r["mode"]), {})[r["threads"]] = r
+    for (kind, cap, mode), pts in keyed.items():
+        cells = []
+        for k in range(args.sweep_min_log2, args.sweep_max_log2 + 1):
+            r = pts.get(1 << k)
+            if r is None:
+                cells.append("")
+            elif r["status"] != "ok":
+                cells.append("n/a" if r["status"].startswith("n/a") else "error")
+            else:
+                cells.append("%.1f%s" % (r["succ_mops"], "" if r.get("fifo") == "YES" else
+                                         (" (fifo skipped)" if r.get("fifo") == "skipped" else " (FIFO NO)")))
+        out.append("| %s | %s | %s | %s |" % (kind, "pool" if cap is None else "2^%d" % cap, mode, " | ".join(cells)))
+    return "\n".join(out) + "\n"
+
+
+def other_workloads(args, local):
+    """The metric's second half beside the queue throughput: graph A BFS
+    traversals/s (asynchronous, 8192 threads; 3 warm-up and 10 timed traversals,
+    depths checked against the serial BFS) and the served mix (traversals/s with
+    p50/p99, one launch per request on the same mix; 3 warm-up and 3 timed runs, the
+    server's configuration fixed at the autotuner's choice).  Each keeps its own
+    timing, parity check and CPU baseline."""
+    import copy
+    keep = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "e2e", "roofline", "parity",
+            "cpu_baseline", "clocks", "gpu_launches")
+    a = copy.copy(args)
+    a.steps, a.warmup = 10, 3
+    bfs = bfs_line(a, local, full=False)
+    out = {"bfs": {k: bfs[k] for k in keep if k in bfs}}
+    out["bfs"]["metric"] = bfs["metric"]
+    a = copy.copy(args)
+    a.steps, a.warmup = 3, 3
+    a.serve_autotune = False
+    a.serve_sample = 2
+    srv = served_line(a, local)
+    sv = {k: srv[k] for k in keep + ("latency_ms", "tiles_per_s", "tiles_per_s_while_served", "poisson",
+                                      "one_launch_per_request", "work") if k in srv}
+    sv["metric"] = srv["metric"]
+    sv["parity"] = "every sampled traversal's checksum, reached count and eccentricity equal the serial BFS; " \
+                   "every tile's checksum equals the serial render's"
+    ol = srv["one_launch_per_request"]
+    sv["served_vs_one_launch_per_request"] = ol["speedup"]
+    # traversals/s served against one launch per traversal of plain G-WFQ (the
+    # reference's level-synchronous traversal; and this build's asynchronous one)
+    if ol.get("traversals_per_s"):
+        sv["served_vs_one_launch_traversals"] = round(srv["value"] / ol["traversals_per_s"], 2)
+    if ol.get("traversals_per_s_async_launch"):
+        sv["served_vs_async_launch_traversals"] = round(srv["value"] / ol["traversals_per_s_async_launch"], 2)
+    out["served"] = sv
+    return out
 
 
 SERVE_METRIC = "served BFS traversals/s (RMAT 16..22 + grids A, B, mixed with ray tiles)"
@@ -558,26 +717,35 @@ BFS_METRIC = "BFS traversals/s (graph A: 4096^2 grid, keep 0.6, diagonals 0.01; 
 
 
 def run_bfs(args):
+    rank, world, local = _env_rank()
+    if rank != 0:
+        return 0   # replicas only
+    print(json.dumps(bfs_line(args, local)), flush=True)
+    return 0
+
+
+def bfs_line(args, local, full=True):
     """BFS with the queue as frontier worklist: graphs A and B from vertex 0, level-
     synchronous (the reference's launch per level) and asynchronous (one persistent
-    launch), 8192 queue threads in blocks of 256, 3 warm-up and 10 timed traversals."""
+    launch), 512 and 8192 queue threads in blocks of 256, 3 warm-up and 10 timed
+    traversals.  full=False times only the headline configuration (graph A,
+    asynchronous, 8192 threads)."""
     import numpy as np
     import gcq_gb300 as g
     from oracle import build as obuild, lib as olib
 
-    rank, world, local = _env_rank()
-    if rank != 0:
-        return 0   # replicas only
     peaks = g.roofline(reps=2)
     graphs = {"A": g.graph_grid(4096, 4096, 0.6, 0.01, 2), "B": g.graph_grid(212, 212, 0.6, 0.01, 2)}
+    if not full:
+        graphs = {"A": graphs["A"]}
     warm, iters = max(3, args.warmup), max(args.steps, 10)
     table, depths = {}, {}
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
     for name, (off, idx) in graphs.items():
-        for mode, persistent in (("level_sync", 0), ("async", 2)):
-            for threads in (512, 8192):
+        for mode, persistent in ((("level_sync", 0), ("async", 2)) if full else (("async", 2),)):
+            for threads in ((512, 8192) if full else (8192,)):
                 with g.Bfs("gwfq", off, idx, threads=threads) as b:
                     for _ in range(warm):
                         b.run(0, persistent=persistent, levels=False)
@@ -628,20 +796,24 @@ def run_bfs(args):
         "cpu_baseline": {"value": round(1.0 / cpu_s["A"], 3), "unit": "traversals/s", "cores": 1, "kind": "port",
                          "sample": "oracle serial BFS (oracle/bfs_serial.cpp) of graph A from vertex 0, once"},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def run_served(args):
+    rank, world, local = _env_rank()
+    if rank != 0:
+        return 0   # replicas only; the served bench runs on one GPU
+    print(json.dumps(served_line(args, local)), flush=True)
+    return 0
+
+
+def served_line(args, local):
     """Served BFS and ray tiles: one persistent kernel per step over the whole
     request set."""
     import numpy as np
     import gcq_gb300 as g
     from oracle import build as obuild, lib as olib
 
-    rank, world, local = _env_rank()
-    if rank != 0:
-        return 0   # replicas only; the served bench runs on one GPU
     scales = [int(x) for x in args.serve_scales.split(",") if x]
     t0 = time.perf_counter()
     graphs, names = _serve_graphs(g, scales)
@@ -834,8 +1006,7 @@ def run_served(args):
                                                    "render per scene scaled to a tile, summed over the mix"},
         "graph_gen_s": round(gen_s, 1),
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def main():
@@ -850,7 +1021,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-queue", action="store_true", help="skip the table of all four queues")
-    ap.add_argument("--workload", choices=["tb", "served-bfs", "rt", "bfs"], default="tb")
+    ap.add_argument("--tb-only", action="store_true",
+                    help="the queue throughput line alone, without the BFS and served results beside it")
+    ap.add_argument("--workload", choices=["tb", "served-bfs", "rt", "bfs", "sweep"], default="tb")
+    ap.add_argument("--sweep-queues", default="gwfq,glfq,wfq,sfq")
+    ap.add_argument("--sweep-min-log2", type=int, default=10)
+    ap.add_argument("--sweep-max-log2", type=int, default=18)
+    ap.add_argument("--sweep-warmup-ms", type=float, default=200.0)
+    ap.add_argument("--sweep-run-ms", type=float, default=1000.0)
+    ap.add_argument("--sweep-md", default="", help="also write the sweep as a markdown table to this file")
     ap.add_argument("--rt-queue", choices=["gwfq", "glfq", "sfq"], default="gwfq")
     ap.add_argument("--serve-tiles", type=int, default=2048, help="ray-tile requests mixed into the served stream")
     ap.add_argument("--serve-requests", type=int, default=1024)
@@ -875,6 +1054,8 @@ def main():
         return run_rt(args)
     if args.workload == "bfs":
         return run_bfs(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
     return run_gpu(args)
 
 
