@@ -1242,13 +1242,14 @@ int oracle_gwf_slow_passed_slot(int reference_rule, uint32_t* deq_out) {
 // values with patience 1, so every operation takes the slow path, checking one peer
 // every `help_delay` operations (1: every operation; a delay longer than the run
 // disables helping, the control case).  The stalled request must be completed by the helpers: its
-// index reaches a worker's dequeue while thread 0 is still stalled.  Thread 0 then
-// resumes its own slow path, which must find the request done and not insert the
-// index again; a final drain must find every value exactly once.  Returns 1 when
-// all of that holds, 0 when it does not, negative for bad arguments.
-// stats[0]: dequeues of the stalled index by workers while thread 0 was stalled,
-// stats[1]: dequeues of it in total, stats[2]: worker values dequeued exactly once,
-// stats[3]: worker values enqueued.
+// index is in the queue while thread 0 is still stalled -- dequeued by a worker, or
+// left in the queue and drained after the workers finish, before thread 0 resumes.
+// Thread 0 then resumes its own slow path, which must find the request done and not
+// insert the index again; a final drain must find every value exactly once.
+// Returns 1 when all of that holds, 0 when it does not, negative for bad arguments.
+// stats[0]: dequeues of the stalled index while thread 0 was stalled (workers and
+// the drain before the resume), stats[1]: dequeues of it in total, stats[2]: worker
+// values dequeued exactly once, stats[3]: worker values enqueued.
 int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_delay, uint64_t* stats) {
     if (threads < 2 || threads > 64 || ops == 0 || ops > 4096 || help_delay == 0 || !stats) return -1;
     gwf::Ring q;
@@ -1283,14 +1284,24 @@ int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_del
         });
     }
     for (auto& th : ths) th.join();
+    // What the workers left in the queue, drained (as worker 1, whose operations
+    // are over) before thread 0 resumes: with the workers' own dequeues it is
+    // everything inserted while thread 0 was stalled.
+    std::vector<u32> left;
+    for (int k = 0; k < (int)(threads * ops + 16); ++k) {
+        const u32 v = q.dequeue_wf(1);
+        if (v == gwf::BOT) break;
+        left.push_back(v);
+    }
     uint64_t seen_while_stalled = 0;
     for (u32 w = 1; w < threads; ++w)
         for (u32 v : got[w]) seen_while_stalled += (v == stalled_index);
+    for (u32 v : left) seen_while_stalled += (v == stalled_index);
     // thread 0 resumes: its own slow path must find the request finished
     q.enqueue_slow(T << 2, stalled_index, r, 0);
     r.pending.store(0);
     r.seq1.store(seq + 1);
-    std::vector<u32> all;
+    std::vector<u32> all(left);
     for (u32 w = 1; w < threads; ++w) all.insert(all.end(), got[w].begin(), got[w].end());
     for (int k = 0; k < (int)(threads * ops + 16); ++k) {
         const u32 v = q.dequeue_wf(0);

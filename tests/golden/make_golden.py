@@ -111,4 +111,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference checkout: the first argument, else $GCQ_REFERENCE_DIR
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("GCQ_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout>  (or set GCQ_REFERENCE_DIR)")
+    main(ref)
