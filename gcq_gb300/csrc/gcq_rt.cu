@@ -11,6 +11,7 @@
 // re-enqueues the next), so the float sums are deterministic too.
 #include <chrono>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gcq_scene.cuh"
@@ -120,6 +121,22 @@ template <> struct rtq<GCQ_GLFQ> {
     __device__ static bool deq(R* q, uint32_t* out, uint32_t) {
         *out = gcq::glf::dequeue(q);
         return *out != gcq::glf::BOT;
+    }
+};
+// YMC (the reference's USE_WFQ tracer, rt_final.cpp:141-170): a per-tile wf_queue
+// with one handle per tile thread, ray indices stored + 1 (0 is WF_BOTTOM).
+// Consumers poll with ymc::try_dequeue, which takes H tickets only below T, so the
+// per-tile cell pool holds one cell per enqueue and the image is exact; the
+// reference's consumers poll with wf_dequeue, whose failed polls each use up a cell.
+template <> struct rtq<GCQ_WFQ> {
+    using R = gcq::ymc::queue;
+    __device__ static bool maybe(const R* q) { return gcq::ld_rlx(&q->T) > gcq::ld_rlx(&q->H); }
+    __device__ static bool enq(R* q, uint32_t idx, uint32_t tid) { return gcq::ymc::enqueue(q, tid, (uint64_t)idx + 1); }
+    __device__ static bool deq(R* q, uint32_t* out, uint32_t) {
+        uint64_t v = 0;
+        if (!gcq::ymc::try_dequeue(q, &v)) return false;
+        *out = (uint32_t)(v - 1);
+        return true;
     }
 };
 template <> struct rtq<GCQ_SFQ> {
@@ -251,6 +268,30 @@ __global__ void k_init_tiles_glf(char* rings, size_t stride, int tiles) {
     for (int t = blockIdx.y; t < tiles; t += gridDim.y)
         gcq::glf::init_slice((gcq::glf::ring*)(rings + (size_t)t * stride), false,
                              (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, (uint64_t)gridDim.x * blockDim.x);
+}
+__global__ void k_init_tiles_sfq(char* rings, size_t stride, int tiles);
+__global__ void k_init_tiles_ymc(char* rings, size_t stride, int tiles) {
+    for (int t = blockIdx.y; t < tiles; t += gridDim.y) {
+        gcq::ymc::queue* q = (gcq::ymc::queue*)(rings + (size_t)t * stride);
+        gcq::ymc::init_slice(q, q->cap_cells, (uint64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                             (uint64_t)gridDim.x * blockDim.x);
+    }
+}
+// Launch f(integral_constant<int, kind>) for the queue kind of a tracer.
+template <typename F>
+void rt_dispatch(int kind, F&& f) {
+    switch (kind) {
+        case GCQ_GWFQ: f(std::integral_constant<int, GCQ_GWFQ>()); break;
+        case GCQ_GLFQ: f(std::integral_constant<int, GCQ_GLFQ>()); break;
+        case GCQ_WFQ: f(std::integral_constant<int, GCQ_WFQ>()); break;
+        default: f(std::integral_constant<int, GCQ_SFQ>()); break;
+    }
+}
+void init_tiles(int kind, char* rings, size_t stride, int tiles, dim3 grid) {
+    if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<grid, 256>>>(rings, stride, tiles);
+    else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<grid, 256>>>(rings, stride, tiles);
+    else if (kind == GCQ_WFQ) k_init_tiles_ymc<<<grid, 256>>>(rings, stride, tiles);
+    else k_init_tiles_sfq<<<grid, 256>>>(rings, stride, tiles);
 }
 __global__ void k_init_tiles_sfq(char* rings, size_t stride, int tiles) {
     for (int t = blockIdx.y; t < tiles; t += gridDim.y)
@@ -415,12 +456,18 @@ void free_tile_rings(tile_rings* tr) {
     tr->dq = nullptr;
 }
 
+// ymc_cells: the cell pool of a YMC tile queue, one cell per enqueue of the tile's
+// rays (its pixels x (bounces + 1)) with a margin; other kinds ignore it.
 int make_tile_rings(int kind, int tiles, int threads_per_tile, uint32_t queue_log2, uint64_t timeout_ns,
-                    tile_rings* tr) {
+                    tile_rings* tr, uint64_t ymc_cells = 0) {
     const uint64_t n = 1ull << queue_log2;
     size_t stride = 0, per_tile = 0;
     int bits = 5;
-    if (kind == GCQ_GWFQ) {
+    if (kind == GCQ_WFQ) {
+        if (ymc_cells == 0) return GCQ_EINVAL;
+        stride = sizeof(gcq::ymc::queue);
+        per_tile = (size_t)threads_per_tile * sizeof(gcq::ymc::handle) + ymc_cells * sizeof(gcq::ymc::cell);
+    } else if (kind == GCQ_GWFQ) {
         if ((uint64_t)threads_per_tile > n) return GCQ_EUNSUPPORTED;
         while ((((uint64_t)1 << bits) - 1) < (uint64_t)threads_per_tile) ++bits;
         stride = sizeof(gcq::gwf::ring);
@@ -466,6 +513,16 @@ int make_tile_rings(int kind, int tiles, int threads_per_tile, uint32_t queue_lo
             r.deq_wait = 0;
             r.stats = nullptr;
             memcpy(&hh[t * stride], &r, sizeof r);
+        } else if (kind == GCQ_WFQ) {
+            gcq::ymc::queue r;
+            memset(&r, 0, sizeof r);
+            r.handles = (gcq::ymc::handle*)tb;
+            r.cells = (gcq::ymc::cell*)(tb + (size_t)threads_per_tile * sizeof(gcq::ymc::handle));
+            r.err = d_err;
+            r.cap_cells = ymc_cells;
+            r.nhandles = (uint32_t)threads_per_tile;
+            r.patience = WF_PATIENCE;
+            memcpy(&hh[t * stride], &r, sizeof r);
         } else if (kind == GCQ_GLFQ) {
             gcq::glf::ring r;
             memset(&r, 0, sizeof r);
@@ -490,10 +547,9 @@ int make_tile_rings(int kind, int tiles, int threads_per_tile, uint32_t queue_lo
     cudaError_t e = cudaMemcpy(dq, hh.data(), hdr_bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(d_err, 0, 4);
     if (e == cudaSuccess) {
-        const dim3 ig((unsigned)std::min<uint64_t>(64, (2 * n + 255) / 256), (unsigned)std::min(tiles, 1024));
-        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(dq, stride, tiles);
-        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(dq, stride, tiles);
-        else k_init_tiles_sfq<<<ig, 256>>>(dq, stride, tiles);
+        const uint64_t work = kind == GCQ_WFQ ? ymc_cells : 2 * n;
+        const dim3 ig((unsigned)std::min<uint64_t>(64, (work + 255) / 256), (unsigned)std::min(tiles, 1024));
+        init_tiles(kind, dq, stride, tiles, ig);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
@@ -657,16 +713,14 @@ struct gcq_rt_ctx {
 
 extern "C" {
 
-// Render one frame (rt_final.cpp:705-1018).  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ
-// (YMC's per-tile pool runs dry under the persistent loop's failed dequeues and
-// drops rays, as the reference's would; it is not offered here).  image receives
-// width*height RGB float pixels (may be NULL).
+// Render one frame (rt_final.cpp:705-1018).  kind: any of the four queues.  image
+// receives width*height RGB float pixels (may be NULL).
 int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
                   int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out) {
     if (!out || width <= 0 || height <= 0 || tiles_x <= 0 || tiles_y <= 0 || threads_per_tile <= 0 ||
         max_bounces < 0 || scene < 0 || scene > 2 || queue_log2 < 4 || queue_log2 > 24)
         return GCQ_EINVAL;
-    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
+    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_WFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
     memset(out, 0, sizeof(*out));
     const int tiles = tiles_x * tiles_y;
     rt_params P;
@@ -685,7 +739,8 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
     build_scene(scene, sph, pln, P);
 
     tile_rings tr;
-    int rc = make_tile_rings(kind, tiles, threads_per_tile, queue_log2, P.timeout_ns, &tr);
+    int rc = make_tile_rings(kind, tiles, threads_per_tile, queue_log2, P.timeout_ns, &tr,
+                             tile_px * ((uint64_t)max_bounces + 1) + 1024);
     if (rc != GCQ_OK) return rc;
     char* dq = tr.dq;
     const size_t stride = tr.stride;
@@ -718,16 +773,12 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
     unsigned long long* d_traced = d_cnt + tiles;
     const int ns = (int)sph.size(), np = (int)pln.size();
     cudaEventRecord(e0);
-    if (kind == GCQ_GWFQ) k_generate<GCQ_GWFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
-    else if (kind == GCQ_GLFQ) k_generate<GCQ_GLFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
-    else k_generate<GCQ_SFQ><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
-    cudaEventRecord(e1);
-    if (kind == GCQ_GWFQ)
-        k_trace<GCQ_GWFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
-    else if (kind == GCQ_GLFQ)
-        k_trace<GCQ_GLFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
-    else
-        k_trace<GCQ_SFQ><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
+    rt_dispatch(kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_generate<K><<<grid, TPB>>>(dq, stride, d_rays, P, d_alive);
+        cudaEventRecord(e1);
+        k_trace<K><<<grid, TPB>>>(dq, stride, d_sph, ns, d_pln, np, d_rays, d_img, P, d_alive, d_traced, d_err);
+    });
     cudaEventRecord(e2);
     cudaError_t ke = cudaEventSynchronize(e2);
     if (ke == cudaSuccess) ke = cudaGetLastError();
@@ -755,6 +806,7 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
     cleanup();
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
+    if (err & GCQ_ERR_POOL) return GCQ_ECAPACITY;   // a YMC tile pool ran dry: rays were dropped
     return leftover ? GCQ_EDEVICE : GCQ_OK;
 }
 
@@ -858,7 +910,7 @@ int gcq_rt_ctx_create(int kind, int scene, int width, int height, int tile_px, i
         max_bounces > 1000 || scene < 0 || scene > 1 || queue_log2 < 4 || queue_log2 > 24 ||
         (int64_t)width * height > (1ll << 30))
         return GCQ_EINVAL;
-    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
+    if (kind != GCQ_GWFQ && kind != GCQ_GLFQ && kind != GCQ_WFQ && kind != GCQ_SFQ) return GCQ_EUNSUPPORTED;
     if ((uint64_t)tile_px * tile_px > (1ull << queue_log2)) return GCQ_ECAPACITY;   // a tile must fit its queue
     gcq_rt_ctx* c = new gcq_rt_ctx();
     bparams& P = c->P;
@@ -879,7 +931,8 @@ int gcq_rt_ctx_create(int kind, int scene, int width, int height, int tile_px, i
     build_bscene(scene, seed, sph, quad, P);
     c->ns = (int)sph.size();
     c->nq = (int)quad.size();
-    int rc = make_tile_rings(kind, c->max_tiles, threads_per_tile, queue_log2, P.timeout_ns, &c->tr);
+    int rc = make_tile_rings(kind, c->max_tiles, threads_per_tile, queue_log2, P.timeout_ns, &c->tr,
+                             (uint64_t)tile_px * tile_px * ((uint64_t)max_bounces + 1) + 1024);
     if (rc != GCQ_OK) { delete c; return rc; }
     const size_t npx = (size_t)width * height, tpx = (size_t)tile_px * tile_px * c->max_tiles;
     if (cudaMalloc(&c->rays, tpx * sizeof(BRay)) != cudaSuccess || cudaMalloc(&c->pix, tpx * sizeof(BPix)) != cudaSuccess ||
@@ -939,10 +992,7 @@ int gcq_rt_ctx_render(gcq_rt_ctx* c, const int32_t* tiles, int ntiles, float* im
     if (ce != cudaSuccess) return gcqi::cuda_fail(ce, "rt render setup", __FILE__, __LINE__);
     const int kind = c->kind;
     if (!c->fresh) {   // re-initialise the rings this render uses
-        const dim3 ig(64u, (unsigned)std::min(ntiles, 1024));
-        if (kind == GCQ_GWFQ) k_init_tiles_gwf<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
-        else if (kind == GCQ_GLFQ) k_init_tiles_glf<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
-        else k_init_tiles_sfq<<<ig, 256>>>(c->tr.dq, c->tr.stride, ntiles);
+        init_tiles(kind, c->tr.dq, c->tr.stride, ntiles, dim3(64u, (unsigned)std::min(ntiles, 1024)));
     }
     c->fresh = false;
     const int TPB = 256;
@@ -952,19 +1002,13 @@ int gcq_rt_ctx_render(gcq_rt_ctx* c, const int32_t* tiles, int ntiles, float* im
     unsigned long long* d_alive = c->cnt;
     unsigned long long* d_traced = c->cnt + c->max_tiles;
     cudaEventRecord(c->e0);
-    if (kind == GCQ_GWFQ) k_bgen<GCQ_GWFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
-    else if (kind == GCQ_GLFQ) k_bgen<GCQ_GLFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
-    else k_bgen<GCQ_SFQ><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
-    cudaEventRecord(c->e1);
-    if (kind == GCQ_GWFQ)
-        k_btrace<GCQ_GWFQ><<<grid, TPB, smem>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
-                                          c->img, P, d_alive, d_traced, c->tr.err);
-    else if (kind == GCQ_GLFQ)
-        k_btrace<GCQ_GLFQ><<<grid, TPB, smem>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
-                                          c->img, P, d_alive, d_traced, c->tr.err);
-    else
-        k_btrace<GCQ_SFQ><<<grid, TPB, smem>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
+    rt_dispatch(kind, [&](auto kc) {
+        constexpr int K = decltype(kc)::value;
+        k_bgen<K><<<grid, TPB>>>(c->tr.dq, c->tr.stride, dl, c->rays, c->pix, P, d_alive);
+        cudaEventRecord(c->e1);
+        k_btrace<K><<<grid, TPB, smem>>>(c->tr.dq, c->tr.stride, dl, c->sph, c->ns, c->quad, c->nq, c->rays, c->pix,
                                          c->img, P, d_alive, d_traced, c->tr.err);
+    });
     cudaEventRecord(c->e2);
     ce = cudaGetLastError();
     if (ce == cudaSuccess) ce = cudaEventSynchronize(c->e2);
@@ -989,6 +1033,7 @@ int gcq_rt_ctx_render(gcq_rt_ctx* c, const int32_t* tiles, int ntiles, float* im
     out->leftover = leftover;
     if (err & GCQ_ERR_TIMEOUT) return GCQ_ETIMEDOUT;
     if (err & (GCQ_ERR_SPIN | GCQ_ERR_TID)) return GCQ_EDEVICE;
+    if (err & GCQ_ERR_POOL) return GCQ_ECAPACITY;   // a YMC tile pool ran dry: rays were dropped
     return leftover ? GCQ_EDEVICE : GCQ_OK;
 }
 

@@ -38,11 +38,6 @@ int main(int argc, char** argv) {
     const int max_bounces = (argc > 2) ? std::atoi(argv[2]) : 4;
     const int threads_per_tile = (argc > 3) ? std::atoi(argv[3]) : 1024;
     const int kind = harness::queue_kind();
-    if (kind == GCQ_WFQ) {
-        std::fprintf(stderr, "ERROR: the WFQ backend is not supported by this ray tracer (its cell pool is not "
-                             "recycled per bounce); use gwfq, glfq or sfq.\n");
-        return 1;
-    }
     const std::string gpu = harness::gpu_name();
     const uint32_t qlog2 = (uint32_t)__builtin_ctz((unsigned)RT_QUEUE_N);
     const int tpb = 256;

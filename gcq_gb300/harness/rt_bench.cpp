@@ -36,10 +36,6 @@ int main(int argc, char** argv) {
     const int threads_per_tile = (argc > 3) ? std::atoi(argv[3]) : 1024;
     const unsigned long long seed = (argc > 4) ? std::strtoull(argv[4], nullptr, 10) : 1ull;
     const int kind = harness::queue_kind();
-    if (kind == GCQ_WFQ) {
-        std::fprintf(stderr, "ERROR: the WFQ backend is not supported by this ray tracer; use gwfq, glfq or sfq.\n");
-        return 1;
-    }
     const std::string gpu = harness::gpu_name();
     const uint32_t qlog2 = (uint32_t)__builtin_ctz((unsigned)RT_QUEUE_N);
     const int tiles_side = (RT_IMG + RT_TILE - 1) / RT_TILE;

@@ -206,11 +206,6 @@ constexpr uint64_t CELL_FULL = 1;
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-// Signed max without a returned value (not waited for).
-__device__ __forceinline__ void red_max_rlx(int* p, int32_t v) {
-    asm volatile("red.relaxed.gpu.global.max.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // Reset an SCQ Threshold to its maximum after a successful enqueue (SCQ's
 // "if Threshold != 3n-1 then Threshold = 3n-1"): a load of the hot word (served by
 // L2 for every lane of a warp at once) and an exchange only when it moved.  A
@@ -220,12 +215,7 @@ __device__ __forceinline__ void red_max_rlx(int* p, int32_t v) {
 // (G-LFQ): every enqueue then sends an atomic to the one word, and the L2 slice
 // serialises them.
 __device__ __forceinline__ void reset_threshold(int* thr, int32_t thr_max) {
-    int32_t v;
-    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(thr) : "memory");
-    if (v != thr_max) {
-        int32_t old;
-        asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(thr), "r"(thr_max) : "memory");
-    }
+    if (ld_rlx(thr) != thr_max) exchange(thr, thr_max);
 }
 
 // Order of an MPMC queue's index return to its free ring.  A consumer's last

@@ -165,6 +165,9 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
     return false;
 }
 
+#ifndef GCQ_GLF_EMPTY_CHECK
+#define GCQ_GLF_EMPTY_CHECK 1
+#endif
 // fq_dequeue, glf_queue.hpp:510-560.  Returns the index or BOT when empty.
 __device__ inline uint32_t dequeue(ring* q) {
     if (ld_rlx(&q->Threshold) < 0) return BOT;
@@ -206,6 +209,11 @@ __device__ inline uint32_t dequeue(ring* q) {
             return BOT;
         }
         if (fetch_add(&q->Threshold, -1) <= 0) return BOT;
+        // the empty exit before a retry ticket, as G-WFQ's (gwf::seen_empty)
+        if (GCQ_GLF_EMPTY_CHECK) {
+            const uint64_t h = ld_acq(&q->Head);
+            if (ld_rlx(&q->Tail) <= h) return BOT;
+        }
     }
     raise_error(c.err, ERR_SPIN);
     return BOT;

@@ -478,6 +478,26 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
 // Dequeue_wf, gwf_ring.hpp:1286-1356.  Returns the index or BOT when empty.
 // With PF the first fast-path attempt also takes a ticket of pf_ctr into *pf_raw
 // (see try_deq); *pf_raw stays 0 when the dequeue returns before taking one.
+// Empty exit before a retry ticket (GCQ_DEQ_EMPTY_CHECK): after a failed fast-path
+// attempt the dequeue returns BOT when no enqueue ticket lies beyond the Head
+// counter (Head read with acquire, then Tail).  At the Tail read Tail <= Head:
+// every entry whose enqueue has completed has a dequeuer holding its ticket,
+// concurrent with this operation, so the queue is empty at that instant -- the
+// exit SCQ takes after a failed ticket when Tail <= H + 1 (gwf_ring.hpp:452-460),
+// taken without spending another ticket.  Without it, consumers that outnumber
+// producers retry failed tickets until their patience runs out, drive Head ahead
+// of Tail and make the producers' tickets fail in turn: split mode with 25 %
+// producers at 8192 threads ran at 81 Mops/s with 115 M retries in 130 M attempts,
+// against 1072 Mops/s and 456 retries with the exit.  Taken before the first
+// ticket as well, the dependent load halved balanced mode (18.8 against 35.8
+// Gops/s at 262144 threads), so only retries pay for it.  0 turns it off.
+#ifndef GCQ_DEQ_EMPTY_CHECK
+#define GCQ_DEQ_EMPTY_CHECK 1
+#endif
+__device__ __forceinline__ bool seen_empty(ring* q, const cfg& c) {
+    const uint64_t h = c.counter(ld_acq(&q->Head));
+    return c.counter(ld_rlx(&q->Tail)) <= h;
+}
 template <bool PF = false>
 __device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr, uint64_t* pf_raw = nullptr) {
     const cfg c = load_cfg(q);
@@ -489,10 +509,12 @@ __device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr
     if (PF) {
         head = try_deq<true>(q, c, &out, tid, pf_ctr, pf_raw);
         if (head == 0) return out;
+        if (GCQ_DEQ_EMPTY_CHECK && seen_empty(q, c)) return BOT;
     }
     for (uint32_t count = c.deq_patience - (PF ? 1u : 0u); --count != 0;) {
         head = try_deq(q, c, &out, tid);
         if (head == 0) return out;
+        if (GCQ_DEQ_EMPTY_CHECK && seen_empty(q, c)) return BOT;
     }
     GCQ_STAT(c, stat::DEQ_SLOW);
     record* r = &c.rec[tid];
@@ -527,6 +549,22 @@ __device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr
 __device__ __forceinline__ bool maybe_nonempty(const ring* q) {
     const uint32_t b = q->thr_bits;
     return (ld_rlx(&q->Tail) >> b) > (ld_rlx(&q->Head) >> b);
+}
+
+// A stronger poll hint (the reference has none): true when the slot of the next
+// Head ticket already holds an index of that ticket's cycle, an entry a dequeue
+// would take now.  A poller that takes Head tickets only then does not race the
+// enqueuers for slots they are still filling -- each such race marks the slot and
+// makes both sides retry, and a slow-path enqueue, whose tickets come one CAS at a
+// time, can lose every one of them to a crowd of pollers.  An enqueuer can also
+// give a ticket up and leave its slot empty for good, so a poller that keeps
+// seeing Tail ahead of Head with an unfilled head slot should dequeue anyway after
+// a few polls (the dequeue marks the slot and moves on).
+__device__ __forceinline__ bool head_ready(const ring* q) {
+    const cfg c = load_cfg(q);
+    const uint64_t h = c.counter(ld_rlx(&q->Head));
+    const uint64_t e = ld_rlx(&c.entry[c.slot_of(h)]);
+    return cycle_cmp(entry::cycle(e), c.cycle_of(h)) == 0 && !entry::empty_index(entry::index(e));
 }
 
 // Dequeue for polling consumers (the reference has none): at most `tries` fast-path

@@ -329,6 +329,57 @@ __device__ inline uint64_t dequeue(queue* q, uint32_t hid) {
     return v;
 }
 
+// Dequeue for polling consumers (the reference has none): it never moves H past T.
+// The lanes of a warp that call it together take consecutive H tickets with one
+// CAS by their leader, and only as many as T - H; each winner then reads its cell,
+// whose enqueuer holds the matching T ticket, until the value lands.  A polling
+// consumer of wf_dequeue on an empty queue takes an H ticket past T every poll and
+// the cell behind it is lost to the pool (no reclamation, wfqueue_hip_opt.hpp:
+// 208-237); with this one the pool holds one cell per enqueue.  Meant for
+// workloads whose enqueues use the fast path (no consumer marks a cell, so
+// enq_fast's CAS succeeds); a cell found marked TOP belongs to an enqueue that went
+// elsewhere, and the lane returns empty-handed.  false: nothing taken.
+__device__ inline bool try_dequeue(queue* q, uint64_t* out) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, (unsigned long long)(uintptr_t)q);
+    const int leader = __ffs(peers) - 1;
+    const unsigned rank = __popc(peers & lanemask_lt());
+    uint64_t base = 0, n = 0;
+    if ((int)lane_id() == leader) {
+        uint64_t h = ld_acq(&q->H);
+        for (int k = 0; k < 8; ++k) {
+            const uint64_t t = ld_acq(&q->T);
+            if (t <= h) break;
+            const uint64_t want = t - h < (uint64_t)__popc(peers) ? t - h : (uint64_t)__popc(peers);
+            const uint64_t old = cas(&q->H, h, h + want);
+            if (old == h) {
+                base = h;
+                n = want;
+                break;
+            }
+            h = old;
+        }
+    }
+    base = __shfl_sync(peers, base, leader);
+    n = __shfl_sync(peers, n, leader);
+    if (rank >= n) return false;
+    const ctx x = load_ctx(q);
+    cell* c = x.find_cell(base + rank);
+    if (!c) return false;   // past the pool: the enqueue holding this ticket failed too (ERR_POOL)
+    backoff bo;
+    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k) {
+        const uint64_t v = ld_acq(&c->val);
+        if (v == TOP) return false;
+        if (v != BOTTOM) {
+            *out = v;
+            return true;
+        }
+        bo.pause(256);
+    }
+    raise_error(x.err, ERR_SPIN);
+    return false;
+}
+
 }  // namespace ymc
 }  // namespace gcq
 

@@ -73,7 +73,7 @@ def test_argument_checks_without_gpu(built_lib):
     cases = [((g.KINDS["gwfq"], 2, 64, 64, 32, 64, 4, 15, 1), g.EINVAL),
              ((g.KINDS["gwfq"], 0, 0, 64, 32, 64, 4, 15, 1), g.EINVAL),
              ((g.KINDS["gwfq"], 0, 64, 64, 32, 64, -1, 15, 1), g.EINVAL),
-             ((g.KINDS["wfq"], 0, 64, 64, 32, 64, 4, 15, 1), g.EUNSUPPORTED),
+             ((7, 0, 64, 64, 32, 64, 4, 15, 1), g.EUNSUPPORTED),
              ((g.KINDS["gwfq"], 0, 64, 64, 32, 64, 4, 9, 1), g.ECAPACITY)]
     for args, want in cases:
         assert L.gcq_rt_bounce_render(*args, img, ctypes.byref(r)) == want, args
@@ -99,7 +99,7 @@ int main(void) {
     gcq_default_knobs(&k);
     gcq_serve_default_cfg(&c);
     if (gcq_create(GCQ_GWFQ, 30, 64, &k, &q) != GCQ_EINVAL) return 2;
-    if (gcq_rt_bounce_render(GCQ_WFQ, 0, 64, 64, 32, 64, 4, 15, 1, 0, &r) != GCQ_EUNSUPPORTED) return 3;
+    if (gcq_rt_bounce_render(GCQ_WFQ, 2, 64, 64, 32, 64, 4, 15, 1, 0, &r) != GCQ_EINVAL) return 3;
     printf("%s|%u|%u\n", gcq_strerror(GCQ_EINVAL), k.help_delay, c.rt_tile_px);
     return 0;
 }

@@ -20,7 +20,7 @@ def cpu_images(oracle_lib):
     return out
 
 
-@pytest.mark.parametrize("kind", ["gwfq", "glfq", "sfq"])
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "wfq", "sfq"])
 @pytest.mark.parametrize("scene", [0, 1])
 def test_rt_reference_scene(gcq, cpu_images, kind, scene):
     # the reference configuration: 1280x720, 8x8 tiles, 1024 threads per tile, 4 bounces
@@ -33,7 +33,7 @@ def test_rt_reference_scene(gcq, cpu_images, kind, scene):
     assert diff.max() <= TOL, (float(diff.max()), int((diff > TOL).sum()))
 
 
-@pytest.mark.parametrize("kind", ["gwfq", "glfq"])
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "wfq"])
 def test_rt_other_tilings(gcq, oracle_lib, kind):
     # uneven tiles, fewer threads per tile than pixels, 2 bounces
     want = np.zeros((240, 320, 3), np.float32)
@@ -44,10 +44,7 @@ def test_rt_other_tilings(gcq, oracle_lib, kind):
     assert np.abs(img - want).max() <= TOL
 
 
-def test_rt_rejects_ymc_and_small_queue(gcq):
-    with pytest.raises(gcq.GcqError) as e:
-        gcq.rt_render("wfq", scene=0)
-    assert e.value.status == gcq.EUNSUPPORTED
+def test_rt_rejects_small_queue(gcq):
     with pytest.raises(gcq.GcqError) as e:
         gcq.rt_render("gwfq", scene=0, queue_log2=12)   # a 160x90 tile does not fit 4096 slots
     assert e.value.status == gcq.ECAPACITY
@@ -76,7 +73,7 @@ def test_rt_compact_deep_tunnel(gcq, oracle_lib):
     assert np.array_equal(img, want)
 
 
-@pytest.mark.parametrize("kind", ["gwfq", "glfq"])
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "wfq"])
 def test_rt_queue_tunnel_scene(gcq, oracle_lib, kind):
     # the queue renderer on the compaction baseline's scene 2, its own shading
     want = np.zeros((180, 320, 3), np.float32)
@@ -110,7 +107,7 @@ def bounce_images(oracle_lib):
     return {s: _bounce_cpu(oracle_lib, s, 1024, 1024, 4) for s in (0, 1)}
 
 
-@pytest.mark.parametrize("kind", ["gwfq", "glfq", "sfq"])
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "wfq", "sfq"])
 @pytest.mark.parametrize("scene", [0, 1])
 def test_rt_bounce_full_size(gcq, bounce_images, kind, scene):
     """The benchmark configuration: 1024x1024, 32x32-pixel tiles, 1024 threads per
@@ -125,7 +122,7 @@ def test_rt_bounce_full_size(gcq, bounce_images, kind, scene):
     assert np.isfinite(img).all()
 
 
-@pytest.mark.parametrize("kind", ["gwfq", "glfq", "sfq"])
+@pytest.mark.parametrize("kind", ["gwfq", "glfq", "wfq", "sfq"])
 @pytest.mark.parametrize("case", [
     dict(width=100, height=70, tile_px=32, threads_per_tile=1024, max_bounces=4, queue_log2=10),  # ragged tiles
     dict(width=96, height=96, tile_px=16, threads_per_tile=40, max_bounces=6, queue_log2=8),      # fewer threads
@@ -140,6 +137,20 @@ def test_rt_bounce_edge_cases(gcq, oracle_lib, kind, case, scene):
     assert np.abs(img - want).max() <= BOUNCE_TOL
 
 
+def test_rt_ymc_reuses_tiles_and_pool(gcq, oracle_lib):
+    """YMC tile queues rendered again from the same context (rings and pools
+    re-initialised between renders), tile lists in another order: the tiles equal
+    the serial render each time and no pool runs dry."""
+    want, _ = _bounce_cpu(oracle_lib, 1, 256, 256, 4)
+    with gcq.RtTiles("wfq", scene=1, width=256, height=256, max_tiles=16) as c:
+        tiles = np.arange(64, dtype=np.int32)
+        for rep in range(2):
+            for chunk in (tiles[::-1][:16], tiles[16:32], tiles[32:48], tiles[48:]):
+                c.render(np.ascontiguousarray(chunk))
+        r, img = c.render(tiles[:16], image=True)
+    assert np.abs(img - want).max() <= BOUNCE_TOL
+
+
 def test_rt_bounce_seed_changes_scene(gcq, oracle_lib):
     a = gcq.rt_bounce_render("gwfq", scene=0, width=128, height=128, seed=1)[1]
     b = gcq.rt_bounce_render("gwfq", scene=0, width=128, height=128, seed=2)[1]
@@ -149,8 +160,7 @@ def test_rt_bounce_seed_changes_scene(gcq, oracle_lib):
 
 
 def test_rt_bounce_rejects(gcq):
-    for kwargs, status in [(dict(kind="wfq"), gcq.EUNSUPPORTED),
-                           (dict(queue_log2=9), gcq.ECAPACITY),          # a 32x32 tile needs 1024 slots
+    for kwargs, status in [(dict(queue_log2=9), gcq.ECAPACITY),          # a 32x32 tile needs 1024 slots
                            (dict(scene=2), gcq.EINVAL),
                            (dict(max_bounces=-1), gcq.EINVAL),
                            (dict(width=0), gcq.EINVAL)]:
