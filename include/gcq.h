@@ -350,7 +350,9 @@ typedef struct gcq_rt_result {
 /* Render one frame of the reference scene `scene` (0 spheres, 1 Cornell-style box;
  * rt_final.cpp:650-684, cameras :849-859) at width x height in tiles_x x tiles_y
  * tiles, threads_per_tile workers and one queue of 2^queue_log2 per tile, up to
- * max_bounces reflections.  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ.  image (may be
+ * max_bounces reflections.  kind: any of the four queues (YMC as the reference's
+ * USE_WFQ tracer, rt_final.cpp:141-170, with one cell pool per tile; a pool that
+ * runs dry returns GCQ_ECAPACITY).  image (may be
  * NULL) receives width*height RGB floats.  Replaces rt_final.cpp:705-1018. */
 int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int tiles_y, int threads_per_tile,
                   int max_bounces, uint32_t queue_log2, float* image, gcq_rt_result* out);
@@ -360,7 +362,7 @@ int gcq_rt_render(int kind, int scene, int width, int height, int tiles_x, int t
  * quad under a sky, scene 1 = a box room with two boxes and a ceiling light; one
  * sample per pixel, 32-byte rays in per-tile ray-bounce queues (tile_px x tile_px
  * pixels, threads_per_tile workers, 2^queue_log2 entries per tile), paths of at most
- * max_bounces scattering events from `seed`.  kind: GCQ_GWFQ, GCQ_GLFQ or GCQ_SFQ.
+ * max_bounces scattering events from `seed`.  kind: any of the four queues.
  * Sampling uses integer PCG and rejection, so the image is reproducible bit for bit
  * on the CPU. */
 int gcq_rt_bounce_render(int kind, int scene, int width, int height, int tile_px, int threads_per_tile,
