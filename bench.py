@@ -151,6 +151,28 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def profile_values(name):
+    """`key: value` lines of a committed ncu summary under profiles/ (the counters
+    an ncu capture of the kernel gave; bench.py cannot run ncu itself).  {} when
+    the file is absent."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return out
+    for line in open(path):
+        line = line.strip().lstrip("-* ")
+        if line.startswith("`") and "`:" in line:
+            k, v = line[1:].split("`:", 1)
+            try:
+                out[k.strip()] = float(v.strip().split()[0].replace(",", ""))
+            except ValueError:
+                pass
+    return out
+
+
+TB_PROFILE = "gwfq_tb_chunk_262144t_traffic.md"
+
+
 def cpu_baseline(seconds=3.0, order=CAPACITY_LOG2):
     """The oracle's G-WFQ (std::atomic, the reference algorithm) on all host cores."""
     from oracle import lib as olib
@@ -401,6 +423,7 @@ def run_gpu(args):
             "frac": round(atom_rate / peak_rs, 4),
             "traffic": None,
             "kernel": "k_tb_chunk<GCQ_GWFQ>",
+            "traffic_source": None,
             "peak_source": "measured in this run by gcq_roofline_measure: max of spread 64-bit "
                            "fetch-add on distinct lines (%.1f G/s) and warp-contiguous words (%.1f G/s)"
                            % (peaks["rs_lines"] / 1e9, peaks["rs_contig"] / 1e9),
@@ -413,6 +436,14 @@ def run_gpu(args):
         mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
         if os.path.exists(mp):
             roof["hbm_peak_gbs_of_measured"] = json.load(open(mp)).get("hbm_gbs")
+        # per-launch counters of one ncu capture of this kernel at this size
+        pv = profile_values(TB_PROFILE)
+        if "dram_bytes_per_launch" in pv:
+            roof["traffic"] = int(pv["dram_bytes_per_launch"])
+            roof["traffic_source"] = "profiles/%s (dram__bytes_read.sum + dram__bytes_write.sum, one launch)" % TB_PROFILE
+        if "l2_atomic_requests_per_launch" in pv:
+            roof["l2_atomic_requests_per_launch"] = int(pv["l2_atomic_requests_per_launch"])
+            roof["l2_atomic_requests_per_op"] = round(pv["l2_atomic_requests_per_launch"] / (succ / args.steps), 3)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "Mops/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms_all / args.steps, 4),

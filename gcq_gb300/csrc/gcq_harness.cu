@@ -73,18 +73,22 @@ __global__ void __launch_bounds__(1024) k_tb_chunk(void* qv, int mode, int produ
         const bool producer = ((uint64_t)tid * 100u / threads) < (uint64_t)producer_percent;
         const bool nb = (mode == 1);   // SFQ: blocking when balanced, non-blocking when split
         const uint64_t stop = Bounded ? *deadline : 0;
+        using O = gcqi::qops_ctx<K>;
+        typename O::ctx cx = O::ctx_begin(q, tid);
+        typename O::ctx* px = GCQ_TB_CTX ? &cx : nullptr;
         for (uint32_t i = 0; i < chunk_ops; ++i) {
             if (Bounded && gcq::globaltimer_ns() > stop) break;
             if (mode == 0 || producer) {
                 const uint32_t p = payloads ? payloads[(uint64_t)i * threads + tid]
                                             : (uint32_t)gcqi::splitmix64(seed ^ (((uint64_t)tid << 32) | i));
-                if (qops<K>::enq(q, qops<K>::tb_value(p), tid, nb)) ++eo; else ++ef;
+                if (O::enq(q, qops<K>::tb_value(p), tid, nb, px)) ++eo; else ++ef;
             }
             if (mode == 0 || !producer) {
                 uint64_t out = 0;
-                if (qops<K>::deq(q, &out, tid, nb) == 1) ++dok; else ++de;
+                if (O::deq(q, &out, tid, nb, px) == 1) ++dok; else ++de;
             }
         }
+        if (GCQ_TB_CTX) O::ctx_end(q, tid, cx);
     }
     block_add_counters(eo, ef, dok, de, ctr);
 }
@@ -237,6 +241,13 @@ __global__ void k_fifo_drain(void* qv, uint32_t threads, uint32_t ops, uint64_t 
     gcq::backoff bo;
     uint64_t t0 = gcq::globaltimer_ns();
     while (gcq::ld_acq(consumed) < total) {
+        // poll through the read-only hint: a YMC dequeue on an empty queue uses up a
+        // cell of its pool
+        if (!qops<K>::maybe(q)) {
+            if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+            bo.pause(512);
+            continue;
+        }
         const int64_t c0 = (int64_t)gcq::fetch_add(clock, 1ull);
         uint64_t v = 0;
         const int r = qops<K>::deq(q, &v, tid, true);
@@ -291,6 +302,13 @@ __global__ void k_fifo_split(void* qv, uint32_t threads, int pct, uint32_t nprod
     gcq::backoff bo;
     uint64_t t0 = gcq::globaltimer_ns();
     while (gcq::ld_acq(consumed) < total) {
+        // poll through the read-only hint: a YMC dequeue on an empty queue uses up a
+        // cell of its pool
+        if (!qops<K>::maybe(q)) {
+            if (gcq::globaltimer_ns() - t0 > timeout_ns) { gcq::raise_error(err, gcq::ERR_TIMEOUT); return; }
+            bo.pause(512);
+            continue;
+        }
         const int64_t c0 = (int64_t)gcq::fetch_add(clock, 1ull);
         uint64_t v = 0;
         const int r = qops<K>::deq(q, &v, tid, true);

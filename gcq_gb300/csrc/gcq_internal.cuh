@@ -58,27 +58,62 @@ __host__ __device__ inline uint64_t splitmix64(uint64_t x) {
 }
 
 // Per-kind adapters used by the harness kernels: the backend shims of
-// throughout_bench.cpp:112-292 and history.cpp:44-144.
+// throughout_bench.cpp:112-292 and history.cpp:44-144.  maybe(q) is a read-only
+// hint (the ticket counters say an entry may be there) for consumers that poll.
 //   enq: true on success (false = full, or a failed non-blocking attempt)
 //   deq: 1 value, 0 empty, 2 failed without effect (SFQ BUSY / timeout)
 template <int K> struct qops;
 
+// Per-thread context of a kernel thread that runs many operations on one queue
+// (ctx_begin / ctx_end around its loop); only G-WFQ keeps one (gwf::thread_ctx).
+struct no_ctx {};
+
+// GCQ_TB_CTX: the throughput chunk keeps G-WFQ's per-thread context (help
+// countdowns in registers, pre-checks skipped after the thread's own enqueue).
+#ifndef GCQ_TB_CTX
+#define GCQ_TB_CTX 1
+#endif
+
 template <> struct qops<GCQ_GWFQ> {
     using Q = gcq::gwf::mpmc;
+    using ctx = gcq::gwf::thread_ctx;
     __device__ static bool enq(Q* q, uint64_t v, uint32_t tid, bool /*nonblocking*/) {
         return gcq::gwf::enqueue_ptr(q, v, tid);
     }
     __device__ static int deq(Q* q, uint64_t* out, uint32_t tid, bool /*nonblocking*/) {
         return gcq::gwf::dequeue_ptr(q, out, tid) ? 1 : 0;
     }
+    __device__ static ctx ctx_begin(Q* q, uint32_t tid) { return gcq::gwf::ctx_load(gcq::gwf::view_of(q), tid); }
+    __device__ static void ctx_end(Q* q, uint32_t tid, const ctx& x) { gcq::gwf::ctx_store(gcq::gwf::view_of(q), tid, x); }
+    __device__ static bool enq(Q* q, uint64_t v, uint32_t tid, bool, ctx* x) {
+        return gcq::gwf::enqueue_ptr(gcq::gwf::view_of(q), v, tid, x);
+    }
+    __device__ static int deq(Q* q, uint64_t* out, uint32_t tid, bool, ctx* x) {
+        return gcq::gwf::dequeue_ptr(gcq::gwf::view_of(q), out, tid, x) ? 1 : 0;
+    }
     __device__ static uint64_t tb_value(uint32_t p) { return p; }
+    __device__ static bool maybe(Q* q) { return gcq::gwf::maybe_nonempty(&q->aq); }
 };
+// The other queues keep no per-thread context.
+template <int K> struct qops_ctx {
+    using ctx = no_ctx;
+    __device__ static ctx ctx_begin(typename qops<K>::Q*, uint32_t) { return ctx(); }
+    __device__ static void ctx_end(typename qops<K>::Q*, uint32_t, const ctx&) {}
+    __device__ static bool enq(typename qops<K>::Q* q, uint64_t v, uint32_t tid, bool nb, ctx*) {
+        return qops<K>::enq(q, v, tid, nb);
+    }
+    __device__ static int deq(typename qops<K>::Q* q, uint64_t* out, uint32_t tid, bool nb, ctx*) {
+        return qops<K>::deq(q, out, tid, nb);
+    }
+};
+template <> struct qops_ctx<GCQ_GWFQ> : qops<GCQ_GWFQ> {};
 
 template <> struct qops<GCQ_GLFQ> {
     using Q = gcq::glf::mpmc;
     __device__ static bool enq(Q* q, uint64_t v, uint32_t, bool) { return gcq::glf::enqueue_ptr(q, v); }
     __device__ static int deq(Q* q, uint64_t* out, uint32_t, bool) { return gcq::glf::dequeue_ptr(q, out) ? 1 : 0; }
     __device__ static uint64_t tb_value(uint32_t p) { return p; }
+    __device__ static bool maybe(Q* q) { return gcq::ld_rlx(&q->aq.Tail) > gcq::ld_rlx(&q->aq.Head); }
 };
 
 template <> struct qops<GCQ_WFQ> {
@@ -92,6 +127,7 @@ template <> struct qops<GCQ_WFQ> {
     }
     // YMC reserves 0 (empty), ~0 and ~0-1: shift the payload into [1, 2^32].
     __device__ static uint64_t tb_value(uint32_t p) { return (uint64_t)p + 1; }
+    __device__ static bool maybe(Q* q) { return gcq::ld_rlx(&q->T) > gcq::ld_rlx(&q->H); }
 };
 
 template <> struct qops<GCQ_SFQ> {
@@ -112,6 +148,7 @@ template <> struct qops<GCQ_SFQ> {
         return 2;
     }
     __device__ static uint64_t tb_value(uint32_t p) { return p; }
+    __device__ static bool maybe(Q* q) { return (int32_t)(gcq::ld_rlx(&q->tail) - gcq::ld_rlx(&q->head)) > 0; }
 };
 
 }  // namespace gcqi

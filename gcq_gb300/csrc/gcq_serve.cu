@@ -63,7 +63,7 @@ constexpr uint32_t MAX_REQ = 1u << 20;
 constexpr uint64_t MAX_ARRIVAL_NS = 60000000000ull;   // schedules span at most a minute
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t POLL_TRIES = 2;    // fast-path attempts per poll of a server queue
-constexpr uint32_t POLL_MISSES = 8;   // polls of an unfilled head slot before a worker dequeues anyway
+constexpr uint32_t POLL_MISSES = 8;   // polls of the same unfilled head slot before a worker dequeues anyway
 
 // A scene served as tiles: the renderer's parameters and geometry, and the image.
 struct srv_scene {
@@ -290,6 +290,7 @@ __global__ void __launch_bounds__(256, 3) k_serve(srv_ctx x) {
     // a completion; one thread going without an item proves nothing
     uint64_t idle_since = 0, idle_mark = 0;
     uint32_t poll_misses = 0;
+    uint64_t poll_head = 0;
     gcq::backoff bo;
     for (uint32_t iter = 0;; ++iter) {
         uint32_t stop = 0;
@@ -309,8 +310,17 @@ __global__ void __launch_bounds__(256, 3) k_serve(srv_ctx x) {
         // only once the head slot holds an entry (head_ready), or after POLL_MISSES
         // polls that saw Tail ahead with the head slot unfilled
         bool ready = false;
-        if (gcq::gwf::maybe_nonempty(&x.workq->aq))
-            ready = gcq::gwf::head_ready(&x.workq->aq) || ++poll_misses >= POLL_MISSES;
+        if (gcq::gwf::maybe_nonempty(&x.workq->aq)) {
+            ready = gcq::gwf::head_ready(&x.workq->aq);
+            if (!ready) {
+                // an unfilled head slot that stays put over POLL_MISSES polls may be an
+                // abandoned ticket: take it (the dequeue marks it and moves on)
+                const uint64_t h = gcq::ld_rlx(&x.workq->aq.Head);
+                poll_misses = (h == poll_head) ? poll_misses + 1 : 0;
+                poll_head = h;
+                ready = poll_misses >= POLL_MISSES;
+            }
+        }
         const bool got = ready && gcq::gwf::try_dequeue_ptr(x.workq, &it, tid, POLL_TRIES);
         if (ready) poll_misses = 0;
         // 1: an edge range of one vertex (lvl = the level it gives), 2: a cleanup sweep,

@@ -416,10 +416,13 @@ __device__ inline void help_dequeue(ring* q, const cfg& c, record* thr, uint32_t
     fence_acq_rel();
     if (!is_enq && ld_rlx(&thr->seq1) == seq) dequeue_slow(q, c, init_head, thr, tid);
 }
-__device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid) {
-    helper_state hs = c.help[tid];
+// With `reg` the countdown is the caller's copy (a thread_ctx below, kept in
+// registers for the kernel's duration) instead of the thread's slot in c.help.
+__device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid, helper_state* reg = nullptr) {
+    helper_state hs = reg ? *reg : c.help[tid];
     if (--hs.nextCheck != 0) {
-        c.help[tid].nextCheck = hs.nextCheck;
+        if (reg) reg->nextCheck = hs.nextCheck;
+        else c.help[tid].nextCheck = hs.nextCheck;
         return;
     }
     record* thr = &c.rec[hs.nextTid];
@@ -429,7 +432,8 @@ __device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid
     }
     hs.nextCheck = (int32_t)c.help_delay;
     hs.nextTid = (hs.nextTid + 1 == c.max_threads) ? 0 : hs.nextTid + 1;
-    c.help[tid] = hs;
+    if (reg) *reg = hs;
+    else c.help[tid] = hs;
 }
 
 // ------------------------------------------------------------------ top level
@@ -442,10 +446,11 @@ __device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid
 // waited for.  Each operation still makes one help check, so a peer's request is
 // still visited within help_delay operations of every thread.
 template <bool Publish = true, bool HelpAfter = false>
-__device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t first_raw = 0) {
+__device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t first_raw = 0,
+                               helper_state* hs = nullptr) {
     const cfg c = load_cfg(q);
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return; }
-    if (!HelpAfter) help_threads(q, c, tid);
+    if (!HelpAfter) help_threads(q, c, tid, hs);
     uint64_t tail = 0;
     for (uint32_t count = c.enq_patience; --count != 0;) {
         if (first_raw) {
@@ -455,7 +460,7 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
             tail = try_enq<Publish>(q, c, index);
         }
         if (tail == 0) {
-            if (HelpAfter) help_threads(q, c, tid);
+            if (HelpAfter) help_threads(q, c, tid, hs);
             return;
         }
     }
@@ -472,25 +477,28 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
     enqueue_slow(q, c, tail_local, index, r, tid);
     st_rel(&r->pending, 0u);
     st_rel(&r->seq1, seq + 1);
-    if (HelpAfter) help_threads(q, c, tid);
+    if (HelpAfter) help_threads(q, c, tid, hs);
 }
 
 // Dequeue_wf, gwf_ring.hpp:1286-1356.  Returns the index or BOT when empty.
 // With PF the first fast-path attempt also takes a ticket of pf_ctr into *pf_raw
 // (see try_deq); *pf_raw stays 0 when the dequeue returns before taking one.
-// Empty exit before a retry ticket (GCQ_DEQ_EMPTY_CHECK): after a failed fast-path
-// attempt the dequeue returns BOT when no enqueue ticket lies beyond the Head
-// counter (Head read with acquire, then Tail).  At the Tail read Tail <= Head:
-// every entry whose enqueue has completed has a dequeuer holding its ticket,
-// concurrent with this operation, so the queue is empty at that instant -- the
-// exit SCQ takes after a failed ticket when Tail <= H + 1 (gwf_ring.hpp:452-460),
-// taken without spending another ticket.  Without it, consumers that outnumber
-// producers retry failed tickets until their patience runs out, drive Head ahead
-// of Tail and make the producers' tickets fail in turn: split mode with 25 %
+// Empty exit before a Head ticket (GCQ_DEQ_EMPTY_CHECK): the dequeue returns BOT
+// when no enqueue ticket lies beyond the Head counter (Head read with acquire, then
+// Tail).  At the Tail read Tail <= Head: every entry whose enqueue has completed has
+// a dequeuer holding its ticket, concurrent with this operation, so the queue is
+// empty at that instant -- the exit SCQ takes after a failed ticket when
+// Tail <= H + 1 (gwf_ring.hpp:452-460), taken without spending a ticket.  It is
+// taken before every retry, and before the first ticket when the Threshold that
+// the dequeue has just read is below its maximum: dequeues have failed since the
+// last enqueue reset it, so the queue has been running empty.  Without it,
+// consumers that outnumber producers spend tickets on an empty queue, drive Head
+// ahead of Tail and make the producers' tickets fail in turn: split mode with 25 %
 // producers at 8192 threads ran at 81 Mops/s with 115 M retries in 130 M attempts,
-// against 1072 Mops/s and 456 retries with the exit.  Taken before the first
-// ticket as well, the dependent load halved balanced mode (18.8 against 35.8
-// Gops/s at 262144 threads), so only retries pay for it.  0 turns it off.
+// against 1072 Mops/s and 456 retries with the exit before every ticket.  Before
+// every first ticket unconditionally, the dependent load halved balanced mode
+// (18.8 against 35.8 Gops/s at 262144 threads), where the Threshold stays at its
+// maximum and the condition keeps the check away.  0 turns it off.
 #ifndef GCQ_DEQ_EMPTY_CHECK
 #define GCQ_DEQ_EMPTY_CHECK 1
 #endif
@@ -498,12 +506,21 @@ __device__ __forceinline__ bool seen_empty(ring* q, const cfg& c) {
     const uint64_t h = c.counter(ld_acq(&q->Head));
     return c.counter(ld_rlx(&q->Tail)) <= h;
 }
+// hs: the caller's register copy of its help countdown (thread_ctx), or null.
+// skip_check: the thread's own last operation on this ring was an enqueue that
+// left Threshold at its maximum, so the pre-check is skipped; it is a hint that
+// spares tickets on an empty queue, and the dequeue stays correct without it.
 template <bool PF = false>
-__device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr, uint64_t* pf_raw = nullptr) {
+__device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr, uint64_t* pf_raw = nullptr,
+                                   helper_state* hs = nullptr, bool skip_check = false) {
     const cfg c = load_cfg(q);
-    if (ld_rlx(&q->Threshold) < 0) return BOT;
+    if (!skip_check) {
+        const int32_t thr = ld_rlx(&q->Threshold);
+        if (thr < 0) return BOT;
+        if (GCQ_DEQ_EMPTY_CHECK && thr != c.threshold_max() && seen_empty(q, c)) return BOT;
+    }
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return BOT; }
-    help_threads(q, c, tid);
+    help_threads(q, c, tid, hs);
     uint32_t out = BOT;
     uint64_t head = 0;
     if (PF) {
@@ -572,9 +589,15 @@ __device__ __forceinline__ bool head_ready(const ring* q) {
 // run out; the caller polls again.  A consumer that polls an idle queue through
 // the wait-free dequeue publishes a slow-path request after deq_patience failures,
 // and with many pollers those requests race the dequeue front without end.
+// A polling consumer makes the help check of every other operation, so that a
+// slow-path request is reached by the pollers too: wCQ completes a request because
+// every thread that keeps operating eventually helps it (gwf_ring.hpp:808-861).
 __device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
-    if (ld_rlx(&q->Threshold) < 0) return BOT;
+    const int32_t thr = ld_rlx(&q->Threshold);
+    if (thr < 0) return BOT;
     const cfg c = load_cfg(q);
+    if (GCQ_DEQ_EMPTY_CHECK && thr != c.threshold_max() && seen_empty(q, c)) return BOT;
+    if (tid < c.max_threads) help_threads(q, c, tid);
     uint32_t out = BOT;
     for (uint32_t k = 0; k < tries; ++k)
         if (try_deq(q, c, &out, tid) == 0) return out;
@@ -604,36 +627,61 @@ struct mpmc_view {
 };
 __device__ __forceinline__ mpmc_view view_of(mpmc* q) { return mpmc_view{&q->aq, &q->fq, q->data, q->err}; }
 
-__device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, uint32_t tid) {
+// Per-thread state of a thread that runs many operations on one queue within a
+// kernel: its two help countdowns (the reference keeps them in the thread's record,
+// gwf_queue.hpp:260-261; here they stay in registers between ctx_load and
+// ctx_store) and, per ring, whether its last operation there was an enqueue that
+// left Threshold at its maximum (the next dequeue skips the pre-check).
+struct thread_ctx {
+    helper_state help_aq, help_fq;
+    bool aq_fresh, fq_fresh;
+};
+__device__ __forceinline__ thread_ctx ctx_load(const mpmc_view& q, uint32_t tid) {
+    thread_ctx x;
+    x.help_aq = q.aq->Help[tid];
+    x.help_fq = q.fq->Help[tid];
+    x.aq_fresh = x.fq_fresh = false;
+    return x;
+}
+__device__ __forceinline__ void ctx_store(const mpmc_view& q, uint32_t tid, const thread_ctx& x) {
+    q.aq->Help[tid] = x.help_aq;
+    q.fq->Help[tid] = x.help_fq;
+}
+
+__device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, uint32_t tid,
+                                            thread_ctx* x = nullptr) {
 #if GCQ_TICKET_PREFETCH
     uint64_t aq_raw = 0;
-    const uint32_t idx = dequeue<true>(q.fq, tid, &q.aq->Tail, &aq_raw);
+    const uint32_t idx = dequeue<true>(q.fq, tid, &q.aq->Tail, &aq_raw, x ? &x->help_fq : nullptr,
+                                       x && x->fq_fresh);
+    if (x) x->fq_fresh = false;
     if (idx == BOT) {
         if (aq_raw) abandon_enq_ticket(q.aq, aq_raw);
         return false;
     }
     put_cell(&q.data[idx], value);
-    enqueue<false>(q.aq, idx, tid, aq_raw);
+    enqueue<false>(q.aq, idx, tid, aq_raw, x ? &x->help_aq : nullptr);
+    if (x) x->aq_fresh = true;
 #else
-    const uint32_t idx = dequeue(q.fq, tid);
+    const uint32_t idx = dequeue(q.fq, tid, nullptr, nullptr, x ? &x->help_fq : nullptr, x && x->fq_fresh);
+    if (x) x->fq_fresh = false;
     if (idx == BOT) return false;
     put_cell(&q.data[idx], value);
-    enqueue<false>(q.aq, idx, tid);
+    enqueue<false>(q.aq, idx, tid, 0, x ? &x->help_aq : nullptr);
+    if (x) x->aq_fresh = true;
 #endif
     return true;
 }
-// Take the cell of index idx and return idx to fq.  The return's release is an
-// acq_rel fence issued as soon as the take has returned (GCQ_RETURN_FENCE, the
-// default), before the enqueue's help bookkeeping writes anything: the fence then
-// waits only for accesses already complete or in flight beside the take, where a
-// release CAS after that bookkeeping waits for its store too.
-#ifndef GCQ_RETURN_FENCE
-#define GCQ_RETURN_FENCE 0
-#endif
+// Take the cell of index idx and return idx to fq.  The return's release is that
+// of an acq_rel CAS.  (An acq_rel fence right after the take, then an acquire CAS,
+// measured slower: 34.0 against 35.5 Gops/s.)  The return's help check runs after
+// its CAS (GCQ_RETURN_HELP_AFTER), so the release does not wait for the store of
+// the help countdown.
 #ifndef GCQ_RETURN_HELP_AFTER
 #define GCQ_RETURN_HELP_AFTER 1
 #endif
-__device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t idx, uint32_t tid) {
+__device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t idx, uint32_t tid,
+                                                    thread_ctx* x = nullptr) {
 #if GCQ_TICKET_PREFETCH
     const uint64_t inc = 1ULL << q.fq->thr_bits;
     const ticket_req t = ticket_issue(&q.fq->Tail, inc);
@@ -645,18 +693,16 @@ __device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t
     const uint64_t v = take_cell(&q.data[idx], q.err);
     const uint64_t fq_raw = 0;
 #endif
-#if GCQ_RETURN_FENCE
-    if (!GCQ_ACQUIRE_ONLY_RETURN) fence_acq_rel();
-    enqueue<false>(q.fq, idx, tid, fq_raw);
-#else
-    enqueue<!GCQ_ACQUIRE_ONLY_RETURN, GCQ_RETURN_HELP_AFTER>(q.fq, idx, tid, fq_raw);
-#endif
+    enqueue<!GCQ_ACQUIRE_ONLY_RETURN, GCQ_RETURN_HELP_AFTER>(q.fq, idx, tid, fq_raw, x ? &x->help_fq : nullptr);
+    if (x) x->fq_fresh = true;
     return v;
 }
-__device__ __forceinline__ bool dequeue_ptr(const mpmc_view& q, uint64_t* out, uint32_t tid) {
-    const uint32_t idx = dequeue(q.aq, tid);
+__device__ __forceinline__ bool dequeue_ptr(const mpmc_view& q, uint64_t* out, uint32_t tid,
+                                            thread_ctx* x = nullptr) {
+    const uint32_t idx = dequeue(q.aq, tid, nullptr, nullptr, x ? &x->help_aq : nullptr, x && x->aq_fresh);
+    if (x) x->aq_fresh = false;
     if (idx == BOT) return false;
-    *out = take_and_return(q, idx, tid);
+    *out = take_and_return(q, idx, tid, x);
     return true;
 }
 __device__ __forceinline__ bool enqueue_ptr(mpmc* q, uint64_t value, uint32_t tid) {
