@@ -866,6 +866,10 @@ def served_line(args, local):
     peaks = g.roofline(reps=2)
     common = dict(budget_bytes=150 << 30, run_limit_s=60.0, rt_scenes=2 if n_tiles else 0,
                   rt_size=(RT_SIZE, RT_SIZE), rt_tile_px=RT_TILE, rt_max_bounces=RT_BOUNCES, rt_seed=RT_SEED)
+    if args.serve_patience == "reference":
+        # the worklist's G-WFQ at the reference's patience (gwf_queue.hpp:300-306): an
+        # operation that keeps failing on the fast path takes the wait-free slow path
+        common.update(enq_patience=128, deq_patience=256)
     tuned, tune_table = dict(threads=args.serve_threads, work_log2=args.serve_work_log2), None
     if args.serve_autotune:
         sample = reqs[: min(len(reqs), 384)].copy()
@@ -999,9 +1003,11 @@ def served_line(args, local):
                                                    if args.serve_rate else "closed-batch"),
         "config": {"workload": "served BFS + ray tiles: %s + scenes 0,1 (1024x1024, 32x32 tiles, 4 bounces); "
                                "%d requests; 150 GiB budget (%d slots, %.1f GB of level arrays); %d persistent "
-                               "threads; worklist 2^%s" % ("+".join(names), len(reqs), info["slots"],
-                                                           info["level_bytes"] / 1e9, info["threads"],
-                                                           tuned.get("work_log2") or "auto"),
+                               "threads; worklist 2^%s; worklist patience %s" % (
+                                   "+".join(names), len(reqs), info["slots"], info["level_bytes"] / 1e9,
+                                   info["threads"], tuned.get("work_log2") or "auto",
+                                   "128/256 (the reference's: wait-free slow path reachable)"
+                                   if args.serve_patience == "reference" else "2^16 (fast path only)"),
                    "graphs": {nm: {"V": v, "E": e} for nm, v, e in zip(names, V, E)},
                    "l2": "inputs larger than L2 (graphs %.1f GB)" % (sum(4 * (v + 1) + 4 * e for v, e in zip(V, E)) / 1e9)},
         "tiles_per_s": round(n_tiles * args.steps / kern_s, 1),
@@ -1072,6 +1078,9 @@ def main():
                     help="worklist capacity log2 (0: the library default, 2^25 raised to 4x the largest graph)")
     ap.add_argument("--no-serve-autotune", dest="serve_autotune", action="store_false",
                     help="use --serve-threads / --serve-work-log2 instead of timing candidates on a sample")
+    ap.add_argument("--serve-patience", choices=["reference", "fast"], default="fast",
+                    help="worklist patience: the reference's 128/256 (wait-free slow path reachable) or "
+                         "2^16 (the library default, fast path only)")
     ap.add_argument("--no-serve-poisson", dest="serve_poisson", action="store_false",
                     help="skip the open-loop Poisson run at 70 %% of the closed-batch rate")
     args = ap.parse_args()

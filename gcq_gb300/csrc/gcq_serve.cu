@@ -63,7 +63,10 @@ constexpr uint32_t MAX_REQ = 1u << 20;
 constexpr uint64_t MAX_ARRIVAL_NS = 60000000000ull;   // schedules span at most a minute
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t POLL_TRIES = 2;    // fast-path attempts per poll of a server queue
-constexpr uint32_t POLL_MISSES = 8;   // polls of the same unfilled head slot before a worker dequeues anyway
+constexpr uint32_t POLL_MISSES = 8;   // polls of an unfilled head slot before a worker dequeues anyway
+// Patience of the worklist by default: its enqueues retry on the fast path and the
+// wait-free slow path is not entered in practice (see gcq_serve_default_cfg).
+constexpr uint32_t SERVER_PATIENCE = 1u << 16;
 
 // A scene served as tiles: the renderer's parameters and geometry, and the image.
 struct srv_scene {
@@ -290,7 +293,6 @@ __global__ void __launch_bounds__(256, 3) k_serve(srv_ctx x) {
     // a completion; one thread going without an item proves nothing
     uint64_t idle_since = 0, idle_mark = 0;
     uint32_t poll_misses = 0;
-    uint64_t poll_head = 0;
     gcq::backoff bo;
     for (uint32_t iter = 0;; ++iter) {
         uint32_t stop = 0;
@@ -310,17 +312,8 @@ __global__ void __launch_bounds__(256, 3) k_serve(srv_ctx x) {
         // only once the head slot holds an entry (head_ready), or after POLL_MISSES
         // polls that saw Tail ahead with the head slot unfilled
         bool ready = false;
-        if (gcq::gwf::maybe_nonempty(&x.workq->aq)) {
-            ready = gcq::gwf::head_ready(&x.workq->aq);
-            if (!ready) {
-                // an unfilled head slot that stays put over POLL_MISSES polls may be an
-                // abandoned ticket: take it (the dequeue marks it and moves on)
-                const uint64_t h = gcq::ld_rlx(&x.workq->aq.Head);
-                poll_misses = (h == poll_head) ? poll_misses + 1 : 0;
-                poll_head = h;
-                ready = poll_misses >= POLL_MISSES;
-            }
-        }
+        if (gcq::gwf::maybe_nonempty(&x.workq->aq))
+            ready = gcq::gwf::head_ready(&x.workq->aq) || ++poll_misses >= POLL_MISSES;
         const bool got = ready && gcq::gwf::try_dequeue_ptr(x.workq, &it, tid, POLL_TRIES);
         if (ready) poll_misses = 0;
         // 1: an edge range of one vertex (lvl = the level it gives), 2: a cleanup sweep,
@@ -612,15 +605,18 @@ void gcq_serve_default_cfg(gcq_serve_cfg* c) {
     c->timeout_ns = 10000000000ull;
     c->run_limit_ns = 60000000000ull;
     c->max_slots = 1024;
-    // The reference's patience (128 / 256): an operation that keeps failing on the
-    // fast path takes the wait-free slow path.  The server polls its worklist from
-    // every resident thread; its workers take a Head ticket only once the head slot
-    // holds an entry (gwf::head_ready), so a slow-path enqueue's tickets are not
-    // lost to a crowd of pollers marking them first.  (Before that hint the slow
-    // path did not complete under about 10^5 pollers and the server kept every
-    // operation on the fast path with a patience of 2^16: 358-364 traversals/s on
-    // the benchmark mix, against 317-329 at the reference's patience with the hint.)
+    // The server polls its worklist from every resident thread; its workers take a
+    // Head ticket only once the head slot holds an entry (gwf::head_ready), so a
+    // slow-path enqueue's tickets are not lost to a crowd of pollers marking them
+    // first.  With that hint the reference's patience (128 / 256, wait-free slow
+    // path reachable) serves the benchmark mix on 65536 workers (317-329 against
+    // 358-364 traversals/s here), but with every resident thread (~117 K) polling, a
+    // slow-path request still stalls past the server's bound.  The default keeps
+    // every operation on the fast path; callers choose the reference's patience
+    // through work_knobs.
     gcq_default_knobs(&c->work_knobs);
+    c->work_knobs.enq_patience = SERVER_PATIENCE;
+    c->work_knobs.deq_patience = SERVER_PATIENCE;
     c->threads = 0;
     c->work_log2 = 0;
     c->rt_scenes = 0;

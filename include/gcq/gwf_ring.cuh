@@ -589,15 +589,9 @@ __device__ __forceinline__ bool head_ready(const ring* q) {
 // run out; the caller polls again.  A consumer that polls an idle queue through
 // the wait-free dequeue publishes a slow-path request after deq_patience failures,
 // and with many pollers those requests race the dequeue front without end.
-// A polling consumer makes the help check of every other operation, so that a
-// slow-path request is reached by the pollers too: wCQ completes a request because
-// every thread that keeps operating eventually helps it (gwf_ring.hpp:808-861).
 __device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
-    const int32_t thr = ld_rlx(&q->Threshold);
-    if (thr < 0) return BOT;
+    if (ld_rlx(&q->Threshold) < 0) return BOT;
     const cfg c = load_cfg(q);
-    if (GCQ_DEQ_EMPTY_CHECK && thr != c.threshold_max() && seen_empty(q, c)) return BOT;
-    if (tid < c.max_threads) help_threads(q, c, tid);
     uint32_t out = BOT;
     for (uint32_t k = 0; k < tries; ++k)
         if (try_deq(q, c, &out, tid) == 0) return out;
