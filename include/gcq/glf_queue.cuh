@@ -177,7 +177,11 @@ __device__ inline uint32_t dequeue(ring* q) {
         // the empty exit before a first ticket while dequeues are failing, as G-WFQ's
         if (GCQ_GLF_EMPTY_CHECK && thr != c.threshold_max()) {
             const uint64_t h = ld_acq(&q->Head);
-            if (ld_rlx(&q->Tail) <= h) return BOT;
+            const uint64_t t = ld_rlx(&q->Tail);
+            if (t <= h) {
+                if (t < h) catchup(q, t, h);
+                return BOT;
+            }
         }
     }
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
@@ -220,7 +224,11 @@ __device__ inline uint32_t dequeue(ring* q) {
         // the empty exit before a retry ticket, as G-WFQ's (gwf::seen_empty)
         if (GCQ_GLF_EMPTY_CHECK) {
             const uint64_t h = ld_acq(&q->Head);
-            if (ld_rlx(&q->Tail) <= h) return BOT;
+            const uint64_t t = ld_rlx(&q->Tail);
+            if (t <= h) {
+                if (t < h) catchup(q, t, h);
+                return BOT;
+            }
         }
     }
     raise_error(c.err, ERR_SPIN);

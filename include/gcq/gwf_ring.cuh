@@ -502,9 +502,15 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
 #ifndef GCQ_DEQ_EMPTY_CHECK
 #define GCQ_DEQ_EMPTY_CHECK 1
 #endif
+// When Head is ahead of Tail (dequeuers spent tickets past the last enqueue), the
+// exit moves Tail up to Head, as SCQ's failing dequeuer does (catchup): otherwise the
+// producers' next tickets land on the passed slots and fail one by one.
 __device__ __forceinline__ bool seen_empty(ring* q, const cfg& c) {
     const uint64_t h = c.counter(ld_acq(&q->Head));
-    return c.counter(ld_rlx(&q->Tail)) <= h;
+    const uint64_t t = c.counter(ld_rlx(&q->Tail));
+    if (t > h) return false;
+    if (t < h) catchup(q, c, t, h);
+    return true;
 }
 // hs: the caller's register copy of its help countdown (thread_ctx), or null.
 // skip_check: the thread's own last operation on this ring was an enqueue that
