@@ -170,20 +170,8 @@ __device__ inline bool enqueue(ring* q, uint32_t index) {
 #endif
 // fq_dequeue, glf_queue.hpp:510-560.  Returns the index or BOT when empty.
 __device__ inline uint32_t dequeue(ring* q) {
+    if (ld_rlx(&q->Threshold) < 0) return BOT;
     const cfg c = load_cfg(q);
-    {
-        const int32_t thr = ld_rlx(&q->Threshold);
-        if (thr < 0) return BOT;
-        // the empty exit before a first ticket while dequeues are failing, as G-WFQ's
-        if (GCQ_GLF_EMPTY_CHECK && thr != c.threshold_max()) {
-            const uint64_t h = ld_acq(&q->Head);
-            const uint64_t t = ld_rlx(&q->Tail);
-            if (t <= h) {
-                if (t < h) catchup(q, t, h);
-                return BOT;
-            }
-        }
-    }
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
         const uint64_t H = warp_ticket(&q->Head, 1);
         const uint32_t hcyc = c.cycle_of(H);

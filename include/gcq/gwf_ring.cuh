@@ -489,16 +489,17 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
 // a dequeuer holding its ticket, concurrent with this operation, so the queue is
 // empty at that instant -- the exit SCQ takes after a failed ticket when
 // Tail <= H + 1 (gwf_ring.hpp:452-460), taken without spending a ticket.  It is
-// taken before every retry, and before the first ticket when the Threshold that
-// the dequeue has just read is below its maximum: dequeues have failed since the
-// last enqueue reset it, so the queue has been running empty.  Without it,
-// consumers that outnumber producers spend tickets on an empty queue, drive Head
-// ahead of Tail and make the producers' tickets fail in turn: split mode with 25 %
-// producers at 8192 threads ran at 81 Mops/s with 115 M retries in 130 M attempts,
-// against 1072 Mops/s and 456 retries with the exit before every ticket.  Before
-// every first ticket unconditionally, the dependent load halved balanced mode
-// (18.8 against 35.8 Gops/s at 262144 threads), where the Threshold stays at its
-// maximum and the condition keeps the check away.  0 turns it off.
+// taken before every retry, and before the first ticket when the caller says its
+// previous dequeue on this ring found the queue empty (first_check, from a
+// thread_ctx).  Without it, consumers that outnumber producers spend tickets on an
+// empty queue, drive Head ahead of Tail and make the producers' tickets fail in
+// turn: split mode with 25 % producers at 8192 threads ran at 81 Mops/s with 115 M
+// retries in 130 M attempts, against 1072 Mops/s and 456 retries with the exit
+// before every ticket.  Before every first ticket unconditionally, the dependent
+// loads halved balanced mode (18.8 against 35.8 Gops/s at 262144 threads), and
+// triggered by the ring's Threshold being below its maximum they sent balanced
+// mode at 262144 threads, stochastically, into a regime of 5.2 ms per chunk
+// against 1.9.  0 turns it off.
 #ifndef GCQ_DEQ_EMPTY_CHECK
 #define GCQ_DEQ_EMPTY_CHECK 1
 #endif
@@ -516,15 +517,14 @@ __device__ __forceinline__ bool seen_empty(ring* q, const cfg& c) {
 // skip_check: the thread's own last operation on this ring was an enqueue that
 // left Threshold at its maximum, so the pre-check is skipped; it is a hint that
 // spares tickets on an empty queue, and the dequeue stays correct without it.
+// first_check: the thread's last dequeue on this ring found it empty, so the empty
+// exit is tried before the first ticket too.
 template <bool PF = false>
 __device__ inline uint32_t dequeue(ring* q, uint32_t tid, u64a* pf_ctr = nullptr, uint64_t* pf_raw = nullptr,
-                                   helper_state* hs = nullptr, bool skip_check = false) {
+                                   helper_state* hs = nullptr, bool skip_check = false, bool first_check = false) {
     const cfg c = load_cfg(q);
-    if (!skip_check) {
-        const int32_t thr = ld_rlx(&q->Threshold);
-        if (thr < 0) return BOT;
-        if (GCQ_DEQ_EMPTY_CHECK && thr != c.threshold_max() && seen_empty(q, c)) return BOT;
-    }
+    if (!skip_check && ld_rlx(&q->Threshold) < 0) return BOT;
+    if (GCQ_DEQ_EMPTY_CHECK && first_check && seen_empty(q, c)) return BOT;
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return BOT; }
     help_threads(q, c, tid, hs);
     uint32_t out = BOT;
@@ -634,13 +634,15 @@ __device__ __forceinline__ mpmc_view view_of(mpmc* q) { return mpmc_view{&q->aq,
 // left Threshold at its maximum (the next dequeue skips the pre-check).
 struct thread_ctx {
     helper_state help_aq, help_fq;
-    bool aq_fresh, fq_fresh;
+    bool aq_fresh, fq_fresh;   // last operation on the ring: this thread's enqueue
+    bool aq_empty, fq_empty;   // last dequeue on the ring: found it empty
 };
 __device__ __forceinline__ thread_ctx ctx_load(const mpmc_view& q, uint32_t tid) {
     thread_ctx x;
     x.help_aq = q.aq->Help[tid];
     x.help_fq = q.fq->Help[tid];
     x.aq_fresh = x.fq_fresh = false;
+    x.aq_empty = x.fq_empty = false;
     return x;
 }
 __device__ __forceinline__ void ctx_store(const mpmc_view& q, uint32_t tid, const thread_ctx& x) {
@@ -653,8 +655,11 @@ __device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, 
 #if GCQ_TICKET_PREFETCH
     uint64_t aq_raw = 0;
     const uint32_t idx = dequeue<true>(q.fq, tid, &q.aq->Tail, &aq_raw, x ? &x->help_fq : nullptr,
-                                       x && x->fq_fresh);
-    if (x) x->fq_fresh = false;
+                                       x && x->fq_fresh, x && x->fq_empty);
+    if (x) {
+        x->fq_fresh = false;
+        x->fq_empty = (idx == BOT);
+    }
     if (idx == BOT) {
         if (aq_raw) abandon_enq_ticket(q.aq, aq_raw);
         return false;
@@ -663,8 +668,12 @@ __device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, 
     enqueue<false>(q.aq, idx, tid, aq_raw, x ? &x->help_aq : nullptr);
     if (x) x->aq_fresh = true;
 #else
-    const uint32_t idx = dequeue(q.fq, tid, nullptr, nullptr, x ? &x->help_fq : nullptr, x && x->fq_fresh);
-    if (x) x->fq_fresh = false;
+    const uint32_t idx = dequeue(q.fq, tid, nullptr, nullptr, x ? &x->help_fq : nullptr, x && x->fq_fresh,
+                                 x && x->fq_empty);
+    if (x) {
+        x->fq_fresh = false;
+        x->fq_empty = (idx == BOT);
+    }
     if (idx == BOT) return false;
     put_cell(&q.data[idx], value);
     enqueue<false>(q.aq, idx, tid, 0, x ? &x->help_aq : nullptr);
@@ -699,8 +708,12 @@ __device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t
 }
 __device__ __forceinline__ bool dequeue_ptr(const mpmc_view& q, uint64_t* out, uint32_t tid,
                                             thread_ctx* x = nullptr) {
-    const uint32_t idx = dequeue(q.aq, tid, nullptr, nullptr, x ? &x->help_aq : nullptr, x && x->aq_fresh);
-    if (x) x->aq_fresh = false;
+    const uint32_t idx = dequeue(q.aq, tid, nullptr, nullptr, x ? &x->help_aq : nullptr, x && x->aq_fresh,
+                                 x && x->aq_empty);
+    if (x) {
+        x->aq_fresh = false;
+        x->aq_empty = (idx == BOT);
+    }
     if (idx == BOT) return false;
     *out = take_and_return(q, idx, tid, x);
     return true;
