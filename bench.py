@@ -1067,7 +1067,7 @@ def main():
     ap.add_argument("--sweep-warmup-ms", type=float, default=200.0)
     ap.add_argument("--sweep-run-ms", type=float, default=1000.0)
     ap.add_argument("--sweep-md", default="", help="also write the sweep as a markdown table to this file")
-    ap.add_argument("--rt-queue", choices=["gwfq", "glfq", "sfq"], default="gwfq")
+    ap.add_argument("--rt-queue", choices=["gwfq", "glfq", "wfq", "sfq"], default="gwfq")
     ap.add_argument("--serve-tiles", type=int, default=2048, help="ray-tile requests mixed into the served stream")
     ap.add_argument("--serve-requests", type=int, default=1024)
     ap.add_argument("--serve-rate", type=float, default=0.0, help="Poisson arrivals per second (0: closed batch)")
