@@ -24,10 +24,7 @@ __global__ void k_init_gwf(gcq::gwf::mpmc* q) {
     const uint64_t n = (uint64_t)gridDim.x * blockDim.x;
     gcq::gwf::init_slice(&q->aq, false, gid, n);
     gcq::gwf::init_slice(&q->fq, true, gid, n);
-    for (uint64_t i = gid; i < (1ull << q->aq.order); i += n) {   // every payload cell empty
-        q->data[i].value = 0;
-        q->data[i].full = 0;
-    }
+    for (uint64_t i = gid; i < (1ull << q->aq.order); i += n) q->data[i] = 0;
     if (gid < 2 * gcq::gwf::stat::COUNT && q->aq.stats) q->aq.stats[gid] = 0;
     if (gid == 0) *q->err = 0;
 }
@@ -207,7 +204,7 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
             const uint64_t o_fr = take((uint64_t)max_threads * sizeof(gcq::gwf::record));
             const uint64_t o_ah = take((uint64_t)max_threads * sizeof(gcq::gwf::helper_state));
             const uint64_t o_fh = take((uint64_t)max_threads * sizeof(gcq::gwf::helper_state));
-            const uint64_t o_d = take(n * sizeof(gcq::cell));
+            const uint64_t o_d = take(n * 8);
             const uint64_t o_ao = take(2 * n * 4), o_fo = take(2 * n * 4);
             const uint64_t o_st = take(2 * gcq::gwf::stat::COUNT * 8);
             q->bytes = align_up(off, A);
@@ -235,7 +232,7 @@ int gcq_create(int kind, uint32_t capacity_log2, uint32_t max_threads, const gcq
             h.aq.stats = (gcq::u64a*)(b + o_st);
             h.fq.stats = h.aq.stats + gcq::gwf::stat::COUNT;
             q->stats = h.aq.stats;
-            h.data = (gcq::cell*)(b + o_d);
+            h.data = (gcq::u64a*)(b + o_d);
             h.err = (gcq::u32a*)(b + o_err);
             q->obj = b + o_hdr;
             q->err = (gcq::u32a*)(b + o_err);

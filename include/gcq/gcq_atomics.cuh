@@ -180,28 +180,6 @@ __device__ __forceinline__ bool cas_upd_rlx(u64a* p, uint64_t* expect, uint64_t 
     *expect = old;
     return ok;
 }
-// 128-bit exchange (atom.exch.b128, sm_90+) of the 16-byte-aligned pair at p;
-// the previous pair is returned in *olo, *ohi.
-template <bool Acquire>
-__device__ __forceinline__ void exch128(u64a* p, uint64_t lo, uint64_t hi, uint64_t* olo, uint64_t* ohi) {
-    if (Acquire)
-        asm volatile("{\n\t.reg .b128 val, old;\n\tmov.b128 val, {%2, %3};\n\t"
-                     "atom.acquire.gpu.global.exch.b128 old, [%4], val;\n\tmov.b128 {%0, %1}, old;\n\t}"
-                     : "=l"(*olo), "=l"(*ohi) : "l"(lo), "l"(hi), "l"(p) : "memory");
-    else
-        asm volatile("{\n\t.reg .b128 val, old;\n\tmov.b128 val, {%2, %3};\n\t"
-                     "atom.relaxed.gpu.global.exch.b128 old, [%4], val;\n\tmov.b128 {%0, %1}, old;\n\t}"
-                     : "=l"(*olo), "=l"(*ohi) : "l"(lo), "l"(hi), "l"(p) : "memory");
-}
-// A payload cell of an indirection queue (G-WFQ's MPMC): the value and a
-// full flag, written by the producer and read-and-emptied by the consumer as one
-// 128-bit atomic each.
-struct alignas(16) cell {
-    u64a value;
-    u64a full;   // CELL_FULL while it holds a payload, 0 once taken
-};
-constexpr uint64_t CELL_FULL = 1;
-
 // OR without a returned value: the issuing thread does not wait for it.
 __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
     asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
@@ -218,16 +196,14 @@ __device__ __forceinline__ void reset_threshold(int* thr, int32_t thr_max) {
     if (ld_rlx(thr) != thr_max) exchange(thr, thr_max);
 }
 
-// Order of an MPMC queue's index return to its free ring.  A consumer's last
-// access to a payload (its read or its take of a cell) must come before the next
-// producer's write to it.  The return carries a release -- a release CAS, or an
-// acq_rel fence followed by the CAS (a release pattern in the PTX memory model) --
-// and the producer obtains the index with an acquire read of the free ring's
-// entry, so under the PTX model the consumer's access precedes the producer's
-// write in causality order.  GCQ_ACQUIRE_ONLY_RETURN=1 makes the return
-// acquire-only: the consumer's access has then completed (its value returned)
-// before the CAS is issued, which orders it on this hardware, but the PTX model
-// gives no cross-thread order without the release.  Off by default.
+// Order of an MPMC queue's index return to its free ring.  A consumer's read of a
+// payload must come before the next producer's write to it.  The return is an
+// acq_rel CAS and the producer obtains the index with an acquire read of the free
+// ring's entry, so under the PTX model the read precedes the write in causality
+// order.  GCQ_ACQUIRE_ONLY_RETURN=1 makes the return acquire-only and the payload
+// read an acquire load: the read is then performed before the CAS is issued, which
+// orders it on this hardware, but the PTX model gives no cross-thread order
+// without the release.  Off by default.
 #ifndef GCQ_ACQUIRE_ONLY_RETURN
 #define GCQ_ACQUIRE_ONLY_RETURN 0
 #endif
@@ -290,30 +266,6 @@ __device__ __forceinline__ void raise_error(u32a* err, unsigned int bits) {
     if (err && (ld_rlx(err) & bits) != bits) fetch_or(err, bits);
 }
 
-// Payload cells.  The reference writes data[idx], fences, then enqueues idx
-// (gwf_ring.hpp:1362-1370): a release, which costs the
-// producer a further L2 round trip on this GPU.  Here the producer writes
-// {value, full} with one 128-bit exchange it does not wait for and enqueues idx
-// with an acquire-only CAS; the consumer that dequeues idx takes the cell with a
-// 128-bit exchange to {0, 0}, retrying while the flag is clear -- the producer's
-// write was issued before the index was published, so it lands in bounded time
-// whatever the producer does next.  A taken cell is empty again before idx
-// returns to the free ring, so a full flag is always the current payload's.  The
-// free ring's acquire load orders the write after the previous take; the take's
-// acquire orders the index's return after it.
-__device__ __forceinline__ void put_cell(cell* c, uint64_t value) {
-    uint64_t olo, ohi;   // not waited for
-    exch128<false>(&c->value, value, CELL_FULL, &olo, &ohi);
-}
-__device__ __forceinline__ uint64_t take_cell(cell* c, u32a* err) {
-    for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k) {
-        uint64_t v, f;
-        exch128<true>(&c->value, 0, 0, &v, &f);
-        if (f == CELL_FULL) return v;
-    }
-    raise_error(err, ERR_SPIN);
-    return 0;
-}
 
 // ---------------------------------------------------------------- tickets
 // Warp-aggregated fetch-and-add: the lanes that are executing this call together

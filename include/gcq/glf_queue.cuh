@@ -226,10 +226,12 @@ __device__ inline uint32_t dequeue(ring* q) {
 // fq_enqueue_ptr / fq_dequeue_ptr, glf_queue.hpp:566-582.  The payload is written
 // before an acq_rel index enqueue (the release publishes it) and read after the
 // dequeue's acquire; the index's return to fq is an acq_rel CAS, whose release
-// orders the read before the next producer's write (GCQ_ACQUIRE_ONLY_RETURN).  (Cells
-// as in G-WFQ measured slower here: 52.6 against 60.1 Gops/s balanced at 262144
-// threads.)  They work on the two rings and the payload array, so the library's
-// queue (mpmc) and the self-contained fq_mpmc_t below run the same code.
+// orders the read before the next producer's write (GCQ_ACQUIRE_ONLY_RETURN).
+// (Payloads in flagged 128-bit cells, written by an exchange the producer does not
+// wait for, with an acquire-only index enqueue, measured slower: 52.6 against 60.1
+// Gops/s balanced at 262144 threads.)  They work on the two rings and the payload
+// array, so the library's queue (mpmc) and the self-contained fq_mpmc_t below run
+// the same code.
 __device__ __forceinline__ bool enqueue_ptr(ring* aq, ring* fq, u64a* data, uint64_t value) {
     const uint32_t idx = dequeue(fq);
     if (idx == BOT) return false;

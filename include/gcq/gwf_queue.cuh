@@ -149,14 +149,12 @@ struct alignas(128) ring {
     u64a* stats;            // operation counters (GCQ_STATS builds), see stat::
 };
 
-// Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345).  The reference
-// keeps data[N] u64 and orders the payload write before the index's enqueue with a
-// fence; here the payload travels in a cell whose full flag the consumer checks
-// (put_cell / take_cell).
+// Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345): data[N] holds
+// the payload of each index.
 struct alignas(128) mpmc {
     ring aq;   // allocated indices, starts empty
     ring fq;   // free indices, starts holding 0..N-1
-    cell* data;
+    u64a* data;
     u32a* err;
 };
 
@@ -261,13 +259,12 @@ struct wf_t {
 };
 
 // Indirection queue (gwf_queue.hpp:338-345) as one object a caller can allocate
-// with sizeof and initialise with wf_mpmc_init.  The payloads are cells of 16 bytes
-// ({value, full}, the library's layout) instead of the reference's 8-byte data[N]:
+// with sizeof and initialise with wf_mpmc_init, with the reference's data[N];
 // Enqueue_Ptr/Dequeue_Ptr run the library's code on it.
 template <typename Config, uint32_t N_PARAM>
 struct wf_mpmc_t {
     using queue_type = wf_t<Config, N_PARAM>;
     queue_type aq;
     queue_type fq;
-    gcq::cell data[N_PARAM];
+    gcq::u64a data[N_PARAM];
 };

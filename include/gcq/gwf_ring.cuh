@@ -605,24 +605,33 @@ __device__ inline uint32_t try_dequeue(ring* q, uint32_t tid, uint32_t tries) {
 }
 
 // Enqueue_Ptr / Dequeue_Ptr, gwf_ring.hpp:1362-1380.  false = full / empty.
-// The payload travels in a cell (put_cell / take_cell), so the index's enqueue to
-// aq publishes nothing and is acquire-only; its return to fq carries a release
-// (it orders the take before the next producer's put; see take_and_return).
+// The reference stores the payload, fences, then enqueues the index, so a consumer
+// that dequeues a value also sees every write the producer made before its
+// Enqueue_Ptr (a queue of pointers to filled records).  Here the index's enqueue
+// to aq is an acq_rel CAS: its release orders the producer's earlier writes and
+// the payload store before the index, and the consumer's acquire load of the aq
+// entry orders its payload read and later reads after them.  The index's return
+// to fq carries a release too (it orders the consumer's payload read before the
+// next producer's store; see take_and_return).  Measured against the earlier form
+// -- payloads in flagged 128-bit cells written by an exchange the producer did not
+// wait for, and an acquire-only aq enqueue that published nothing else -- this one
+// is faster as well: 1.70 against 1.99 ms per chunk (balanced, 262144 threads,
+// capacity 2^20, L2 flushed).
 // With GCQ_TICKET_PREFETCH (default) each operation takes its second ring's ticket
 // while the first ring's access is in flight: Enqueue_Ptr issues the aq Tail
 // fetch-and-add beside the fq slot load, Dequeue_Ptr issues the fq Tail
-// fetch-and-add beside the cell's take.  Each saves one dependent L2 round trip.
+// fetch-and-add beside the payload read.  Each saves one dependent L2 round trip.
 //
 // The operations work on a view of an indirection queue -- its two rings, its
-// cells and its error word -- so the library's queue (mpmc) and the compile-time
-// wf_mpmc_t below run the same code.
+// payload array and its error word -- so the library's queue (mpmc) and the
+// compile-time wf_mpmc_t below run the same code.
 #ifndef GCQ_TICKET_PREFETCH
 #define GCQ_TICKET_PREFETCH 1
 #endif
 struct mpmc_view {
     ring* aq;
     ring* fq;
-    cell* data;
+    u64a* data;
     u32a* err;
 };
 __device__ __forceinline__ mpmc_view view_of(mpmc* q) { return mpmc_view{&q->aq, &q->fq, q->data, q->err}; }
@@ -664,8 +673,8 @@ __device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, 
         if (aq_raw) abandon_enq_ticket(q.aq, aq_raw);
         return false;
     }
-    put_cell(&q.data[idx], value);
-    enqueue<false>(q.aq, idx, tid, aq_raw, x ? &x->help_aq : nullptr);
+    st_rlx(&q.data[idx], value);
+    enqueue<true>(q.aq, idx, tid, aq_raw, x ? &x->help_aq : nullptr);
     if (x) x->aq_fresh = true;
 #else
     const uint32_t idx = dequeue(q.fq, tid, nullptr, nullptr, x ? &x->help_fq : nullptr, x && x->fq_fresh,
@@ -675,31 +684,30 @@ __device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, 
         x->fq_empty = (idx == BOT);
     }
     if (idx == BOT) return false;
-    put_cell(&q.data[idx], value);
-    enqueue<false>(q.aq, idx, tid, 0, x ? &x->help_aq : nullptr);
+    st_rlx(&q.data[idx], value);
+    enqueue<true>(q.aq, idx, tid, 0, x ? &x->help_aq : nullptr);
     if (x) x->aq_fresh = true;
 #endif
     return true;
 }
-// Take the cell of index idx and return idx to fq.  The return's release is that
-// of an acq_rel CAS.  (An acq_rel fence right after the take, then an acquire CAS,
-// measured slower: 34.0 against 35.5 Gops/s.)  The return's help check runs after
-// its CAS (GCQ_RETURN_HELP_AFTER), so the release does not wait for the store of
-// the help countdown.
+// Read the payload of index idx and return idx to fq.  The return's release is
+// that of an acq_rel CAS.  (An acq_rel fence right after the read, then an acquire
+// CAS, measured slower.)  The return's help check runs after its CAS
+// (GCQ_RETURN_HELP_AFTER), so the release does not wait for the store of the help
+// countdown.
 #ifndef GCQ_RETURN_HELP_AFTER
 #define GCQ_RETURN_HELP_AFTER 1
 #endif
 __device__ __forceinline__ uint64_t take_and_return(const mpmc_view& q, uint32_t idx, uint32_t tid,
                                                     thread_ctx* x = nullptr) {
+    // the aq entry's acquire load (or, opt-in, this acquire) orders the read
 #if GCQ_TICKET_PREFETCH
     const uint64_t inc = 1ULL << q.fq->thr_bits;
     const ticket_req t = ticket_issue(&q.fq->Tail, inc);
-    uint64_t v, f;
-    exch128<true>(&q.data[idx].value, 0, 0, &v, &f);
+    const uint64_t v = GCQ_ACQUIRE_ONLY_RETURN ? ld_acq(&q.data[idx]) : ld_rlx(&q.data[idx]);
     const uint64_t fq_raw = ticket_take(t, inc);
-    if (f != CELL_FULL) v = take_cell(&q.data[idx], q.err);
 #else
-    const uint64_t v = take_cell(&q.data[idx], q.err);
+    const uint64_t v = GCQ_ACQUIRE_ONLY_RETURN ? ld_acq(&q.data[idx]) : ld_rlx(&q.data[idx]);
     const uint64_t fq_raw = 0;
 #endif
     enqueue<!GCQ_ACQUIRE_ONLY_RETURN, GCQ_RETURN_HELP_AFTER>(q.fq, idx, tid, fq_raw, x ? &x->help_fq : nullptr);
@@ -733,10 +741,10 @@ __device__ __forceinline__ bool dequeue_ptr(mpmc* q, uint64_t* out, uint32_t tid
 __device__ inline bool enqueue_ptr_lockfree(mpmc* q, uint64_t value, uint32_t tid, uint32_t tries) {
     const uint32_t idx = try_dequeue(&q->fq, tid, tries);
     if (idx == BOT) return false;
-    put_cell(&q->data[idx], value);
+    st_rlx(&q->data[idx], value);
     const cfg c = load_cfg(&q->aq);
     for (uint32_t k = 0; k < GCQ_SPIN_LIMIT; ++k)
-        if (try_enq<false>(&q->aq, c, idx) == 0) return true;
+        if (try_enq<true>(&q->aq, c, idx) == 0) return true;
     raise_error(c.err, ERR_SPIN);
     return false;
 }
@@ -791,12 +799,12 @@ __device__ void wf_init(wf_t<Config, N_PARAM>* q, bool full = false) {
     gcq::gwf::init_slice(h, full, 0, 1);
     __threadfence();
 }
-// wf_mpmc_init, gwf_ring.hpp:278-298: aq empty, fq holding 0..N-1, every cell empty.
+// wf_mpmc_init, gwf_ring.hpp:278-298: aq empty, fq holding 0..N-1.
 template <typename Config, uint32_t N_PARAM>
 __device__ void wf_mpmc_init(wf_mpmc_t<Config, N_PARAM>* q) {
     wf_init(&q->aq, false);
     wf_init(&q->fq, true);
-    for (uint32_t i = 0; i < N_PARAM; ++i) { q->data[i].value = 0; q->data[i].full = 0; }
+    for (uint32_t i = 0; i < N_PARAM; ++i) q->data[i] = 0;
     __threadfence();
 }
 template <typename Config, uint32_t N_PARAM>

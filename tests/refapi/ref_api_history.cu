@@ -112,3 +112,119 @@ extern "C" int ref_api_history(int kind, int threads, int ops, rec* out) {
     return (int)e;
 }
 
+// ------------------------------------------------------------------ publication
+// A queue of record ids, as a program that hands filled records from producers to
+// consumers uses it: a producer writes the four words of record `id` with plain
+// stores, then enqueues id; a consumer dequeues an id and reads the record with
+// plain loads.  The reference publishes the producer's writes with its enqueue
+// (Enqueue_Ptr's __threadfence before the index enqueue, gwf_ring.hpp:1362-1369;
+// fq_enqueue_ptr's ordered index enqueue, glf_queue.hpp:566-572; the cell CAS of
+// wf_enqueue; SFQ's slot store), so every record must read complete.  The first
+// half of the blocks produce, the second half consume; waits end at a deadline
+// on the device clock.  cnt: [0] records received, [1] records read incomplete,
+// [2] threads that gave up at the deadline, [3] ids received more than once.
+__device__ __forceinline__ uint64_t now_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint64_t rec_word(uint64_t id, int k) {
+    return (id * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(k + 1) << 56) ^ (id << (8 * k));
+}
+__global__ void publish(int kind, void* qv, void* hv, int per, uint64_t* recs, unsigned* seen,
+                        unsigned long long* cnt, uint64_t budget_ns) {
+    const uint64_t deadline = now_ns() + budget_ns;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t half = (gridDim.x / 2) * blockDim.x;
+    const unsigned long long total = (unsigned long long)half * per;
+    wf_handle* wh = (wf_handle*)hv;
+    if (tid < half) {
+        for (int i = 0; i < per; ++i) {
+            const uint64_t id = (uint64_t)tid * per + i + 1;
+            for (int k = 0; k < 4; ++k) recs[4 * id + k] = rec_word(id, k);
+            uint32_t ns = 32;
+            for (;;) {
+                bool ok;
+                if (kind == 0) ok = Enqueue_Ptr((gwf_q*)qv, id);
+                else if (kind == 1) ok = fq_enqueue_ptr((fq_mpmc_t*)qv, id);
+                else if (kind == 2) ok = wf_enqueue((wf_queue*)qv, &wh[tid], id);
+                else ok = sfq_enqueue_nb_u32((sfq_queue*)qv, (uint32_t)id) == SFQ_SUCCESS;
+                if (ok) break;
+                if (now_ns() > deadline) { atomicAdd(&cnt[2], 1ull); return; }
+                __nanosleep(ns);
+                ns = ns < 2048 ? 2 * ns : ns;
+            }
+        }
+        return;
+    }
+    uint32_t ns = 32;
+    while (*(volatile unsigned long long*)&cnt[0] < total) {
+        if (now_ns() > deadline) { atomicAdd(&cnt[2], 1ull); return; }
+        uint64_t id = 0;
+        if (kind == 0) { if (!Dequeue_Ptr((gwf_q*)qv, &id)) id = 0; }
+        else if (kind == 1) { if (!fq_dequeue_ptr((fq_mpmc_t*)qv, &id)) id = 0; }
+        else if (kind == 2) id = wf_dequeue((wf_queue*)qv, &wh[tid]);
+        else { uint32_t v = 0; if (sfq_dequeue_nb_u32((sfq_queue*)qv, &v) == SFQ_SUCCESS) id = v; }
+        if (id == 0) {
+            __nanosleep(ns);
+            ns = ns < 2048 ? 2 * ns : ns;
+            continue;
+        }
+        ns = 32;
+        bool good = id <= total;
+        for (int k = 0; good && k < 4; ++k) good = recs[4 * id + k] == rec_word(id, k);
+        if (!good) atomicAdd(&cnt[1], 1ull);
+        else if (atomicAdd(&seen[id], 1u) != 0) atomicAdd(&cnt[3], 1ull);
+        atomicAdd(&cnt[0], 1ull);
+    }
+}
+
+// `blocks` blocks of `threads` (blocks even, all resident), `per` records per
+// producer; out receives cnt[0..3] and the expected total.  0, or the failing
+// CUDA error.
+extern "C" int ref_api_publish(int kind, int blocks, int threads, int per, unsigned long long* out) {
+    if (kind < 0 || kind > 3 || blocks < 2 || (blocks & 1) || threads <= 0 || threads > 1024 || per <= 0) return -1;
+    const int nthreads = blocks * threads;
+    const unsigned long long total = (unsigned long long)(blocks / 2) * threads * per;
+    if (total >= (kind == 1 ? FQ_N : 32768u)) return -1;   // under every queue's capacity
+    void* q = nullptr;
+    void* h = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (kind == 0) {
+        if ((e = cudaMalloc(&q, sizeof(gwf_q))) != cudaSuccess) return e;
+        init_gwf<<<1, 1>>>((gwf_q*)q);
+    } else if (kind == 1) {
+        if ((e = cudaMalloc(&q, sizeof(fq_mpmc_t))) != cudaSuccess) return e;
+        init_glf<<<1, 1>>>((fq_mpmc_t*)q);
+    } else if (kind == 2) {
+        e = wf_queue_host_init((wf_queue**)&q, (wf_handle**)&h, nthreads);
+    } else {
+        e = sfq_queue_host_init((sfq_queue**)&q, (sfq_handle**)&h, nthreads);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    uint64_t* recs = nullptr;
+    unsigned long long* cnt = nullptr;
+    unsigned* seen = nullptr;
+    const size_t rbytes = (size_t)(total + 1) * 4 * sizeof(uint64_t);
+    if (e == cudaSuccess) e = cudaMalloc(&recs, rbytes);
+    if (e == cudaSuccess) e = cudaMemset(recs, 0, rbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&seen, (size_t)(total + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(seen, 0, (size_t)(total + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&cnt, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(cnt, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        publish<<<blocks, threads>>>(kind, q, h, per, recs, seen, cnt, 2000000000ull);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(out, cnt, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    out[4] = total;
+    if (recs) cudaFree(recs);
+    if (cnt) cudaFree(cnt);
+    if (seen) cudaFree(seen);
+    if (kind == 2) wf_queue_host_destroy((wf_queue*)q, (wf_handle*)h);
+    else if (kind == 3) sfq_queue_destroy((sfq_queue*)q, (sfq_handle*)h);
+    else if (q) cudaFree(q);
+    return (int)e;
+}

@@ -74,3 +74,24 @@ def test_reference_api_history_linearizable(oracle_lib, kind):
         order = np.lexsort((recs["op"], recs["proc"], recs["end"], recs["call"]))
         v = oracle_lib.check(recs[order], timeout_s=60.0)
         assert v == "Linearizable (FIFO)", (v, oracle_lib.patterns(recs[order]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", sorted(KINDS))
+def test_reference_api_publishes_producer_writes(kind):
+    """A queue of record ids between producer and consumer blocks: each producer
+    fills a 32-byte record with plain stores and enqueues its id; each consumer
+    dequeues ids and reads the records with plain loads.  The reference's enqueues
+    publish the producer's earlier writes (gwf_ring.hpp:1362-1369 fences before the
+    index enqueue), so no record may read incomplete, and every id arrives once."""
+    L = C.CDLL(_build())
+    L.ref_api_publish.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.ref_api_publish.restype = C.c_int
+    for rep in range(3):
+        out = np.zeros(5, dtype=np.uint64)
+        rc = L.ref_api_publish(KINDS[kind], 8, 256, 8, out.ctypes.data)
+        assert rc == 0, "CUDA error %d" % rc
+        received, incomplete, gave_up, twice, total = (int(x) for x in out)
+        assert gave_up == 0, out
+        assert received == total == 4 * 256 * 8, out
+        assert incomplete == 0 and twice == 0, out
