@@ -213,6 +213,12 @@ __global__ void k_bfs_source(void* q, int* level, int src, bfs_misc* m) {
 constexpr int ASYNC_HUB_DEG = 2048;
 constexpr int CHUNK_EDGES = 1024;
 constexpr uint64_t CHUNK_FLAG = 1ull << 63;
+// A thread's edges are relaxed GCQ_BFS_RELAX_BATCH at a time: their
+// neighbour ids are loaded, then their atomicMins issued back to back, so one
+// vertex costs about two dependent round trips instead of one per edge.
+#ifndef GCQ_BFS_RELAX_BATCH
+#define GCQ_BFS_RELAX_BATCH 4
+#endif
 
 struct bfs_async_ctl {
     unsigned long long pending;
@@ -312,8 +318,18 @@ __global__ void __launch_bounds__(256) k_bfs_async(void* qv, const int* __restri
                     n_edges += (unsigned long long)(end - beg);
                     const uint32_t lv = lvl + 1;
                     uint32_t won = 0;
-                    for (int e = beg; e < end; ++e)
-                        if (atomicMin(&level[idx[e]], lv) > lv) won |= 1u << (e - beg);
+                    for (int e0 = beg; e0 < end; e0 += GCQ_BFS_RELAX_BATCH) {
+                        uint32_t w[GCQ_BFS_RELAX_BATCH], old[GCQ_BFS_RELAX_BATCH];
+#pragma unroll
+                        for (int j = 0; j < GCQ_BFS_RELAX_BATCH; ++j)
+                            if (e0 + j < end) w[j] = (uint32_t)idx[e0 + j];
+#pragma unroll
+                        for (int j = 0; j < GCQ_BFS_RELAX_BATCH; ++j)
+                            if (e0 + j < end) old[j] = atomicMin(&level[w[j]], lv);
+#pragma unroll
+                        for (int j = 0; j < GCQ_BFS_RELAX_BATCH; ++j)
+                            if (e0 + j < end && old[j] > lv) won |= 1u << (e0 + j - beg);
+                    }
                     const uint32_t kids = (uint32_t)__popc(won);
                     if (kids > 1) gcq::fetch_add((gcq::u64a*)&c->pending, (uint64_t)kids - 1);
                     for (uint32_t mm = won; mm; mm &= mm - 1)
