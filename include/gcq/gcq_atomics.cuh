@@ -195,14 +195,6 @@ __device__ __forceinline__ void red_or_rlx(u64a* p, uint64_t v) {
 __device__ __forceinline__ void reset_threshold(int* thr, int32_t thr_max) {
     if (ld_rlx(thr) != thr_max) exchange(thr, thr_max);
 }
-// The same reset for a Threshold followed by a 32-bit word in one aligned 8-byte
-// pair (G-WFQ's Announce): one 64-bit load reads both, and the second word is
-// returned.  The GPU is little-endian: Threshold is the low half.
-__device__ __forceinline__ uint32_t reset_threshold_pair(int* thr, int32_t thr_max) {
-    const uint64_t w = ld_rlx((const u64a*)thr);
-    if ((int32_t)(uint32_t)w != thr_max) exchange(thr, thr_max);
-    return (uint32_t)(w >> 32);
-}
 
 // Order of an MPMC queue's index return to its free ring.  A consumer's read of a
 // payload must come before the next producer's write to it.  The return is an

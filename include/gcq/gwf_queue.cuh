@@ -24,7 +24,6 @@
 //     2^18 threads costs 2^18 dependent loads per consume.
 #pragma once
 
-#include <stddef.h>
 #include <stdint.h>
 #include "gcq_atomics.cuh"
 
@@ -133,11 +132,7 @@ struct alignas(128) ring {
     u64a Head;
     char _pad1[GCQ_HOT_STRIDE - 8];
     int Threshold;
-    u32a Announce;          // 1 + index of a thread whose slow-path enqueue asks the
-                            // fast-path enqueuers for help (0: none); shares an 8-byte
-                            // word with Threshold, so the load after every enqueue
-                            // reads both
-    char _pad2[GCQ_HOT_STRIDE - 8];
+    char _pad2[GCQ_HOT_STRIDE - 4];
     u64a* Entry;            // 2N slots
     record* Record;         // max_threads shared records
     helper_state* Help;     // max_threads private countdowns
@@ -153,8 +148,6 @@ struct alignas(128) ring {
     uint32_t _pad4;
     u64a* stats;            // operation counters (GCQ_STATS builds), see stat::
 };
-static_assert(offsetof(ring, Threshold) % 8 == 0 && offsetof(ring, Announce) == offsetof(ring, Threshold) + 4,
-              "Threshold and Announce form one aligned 8-byte word");
 
 // Indirection queue with 64-bit payloads (gwf_queue.hpp:338-345): data[N] holds
 // the payload of each index.

@@ -48,7 +48,6 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
         q->Head = c.pack_global(start, c.null_tid());
         q->Tail = c.pack_global(full ? start + n : start, c.null_tid());
         q->Threshold = full ? c.threshold_max() : -1;
-        q->Announce = 0;
     }
 }
 
@@ -113,15 +112,14 @@ __device__ inline void catchup(ring* q, const cfg& c, uint64_t tail_raw, uint64_
 
 // ------------------------------------------------------------------ fast path
 // try_enq, gwf_ring.hpp:382-414, on ticket T (a Tail counter value).  0 on
-// success, else T.  On success *ann (when given) receives the ring's Announce word,
-// read together with Threshold.
+// success, else T.
 // Publish: the caller wrote what the index refers to before this call, and the
 // entry CAS is acq_rel -- release orders those writes before the index, acquire
 // orders the Threshold reset after the CAS.  Without Publish the caller has ordered
 // its earlier accesses itself, and the CAS is acquire only: a release costs a
 // further L2 round trip on this GPU, an acquire nothing measurable.
 template <bool Publish = true>
-__device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uint64_t T, uint32_t* ann = nullptr) {
+__device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uint64_t T) {
     GCQ_STAT(c, stat::TRY_ENQ);
     const uint32_t tcyc = c.cycle_of(T);
     const uint32_t j = c.slot_of(T);
@@ -132,8 +130,7 @@ __device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uin
     // have read, so the code below continues from it.  Saves one L2 round trip.
     uint64_t E = entry::pack(0xFF, tcyc - 1, true, true, BOT_C);
     if (cas_upd_ord<Publish>(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
-        const uint32_t a = reset_threshold_pair(&q->Threshold, c.threshold_max());
-        if (ann) *ann = a;
+        reset_threshold(&q->Threshold, c.threshold_max());
         return 0;
     }
     for (uint32_t spin = 0; spin < GCQ_SPIN_LIMIT; ++spin) {
@@ -146,16 +143,15 @@ __device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uin
         }
         const uint64_t nw = entry::pack(entry::note(E), tcyc, true, true, index);
         if (!cas_upd_ord<Publish>(&c.entry[j], &E, nw)) continue;
-        const uint32_t a = reset_threshold_pair(&q->Threshold, c.threshold_max());
-        if (ann) *ann = a;
+        reset_threshold(&q->Threshold, c.threshold_max());
         return 0;
     }
     raise_error(c.err, ERR_SPIN);
     return T;
 }
 template <bool Publish = true>
-__device__ __forceinline__ uint64_t try_enq(ring* q, const cfg& c, uint32_t index, uint32_t* ann = nullptr) {
-    return try_enq_at<Publish>(q, c, index, c.counter(warp_ticket(&q->Tail, c.cinc())), ann);
+__device__ __forceinline__ uint64_t try_enq(ring* q, const cfg& c, uint32_t index) {
+    return try_enq_at<Publish>(q, c, index, c.counter(warp_ticket(&q->Tail, c.cinc())));
 }
 
 // An enqueue ticket taken ahead of need and then not used (the operation it was for
@@ -449,44 +445,6 @@ __device__ __forceinline__ void help_threads(ring* q, const cfg& c, uint32_t tid
 // the help check writes the thread's countdown: after the CAS, that store is not
 // waited for.  Each operation still makes one help check, so a peer's request is
 // still visited within help_delay operations of every thread.
-//
-// Announced requests (GCQ_ANNOUNCE, default on).  A slow-path enqueue takes its
-// tickets from Tail with a CAS, which fails whenever a fast-path fetch-and-add
-// lands in between; with 10^4-10^5 producers on the fast path it can fail for
-// seconds, long before the round-robin help check (one peer every help_delay
-// operations) reaches its record.  So the request is also announced in the ring's
-// Announce word (a CAS from 0; one request at a time, others rely on the
-// round-robin), and every successful fast-path enqueue, which reads that word
-// together with Threshold, helps the announced request before it returns.  The
-// producers then join the request's cooperative fetch-and-add instead of
-// advancing Tail past it, and it completes.  The word is cleared when the request
-// is over; a helper that reads a stale value finds the request over (seq1 moved or
-// pending clear) and returns at once.
-#ifndef GCQ_ANNOUNCE
-#define GCQ_ANNOUNCE 1
-#endif
-// GCQ_ANNOUNCE_LEADER: of the lanes of a warp that read the announcement together,
-// the lowest helps and the others wait (bounded) for the word to change, instead
-// of every lane running the slow path's CASes on the same words.
-#ifndef GCQ_ANNOUNCE_LEADER
-#define GCQ_ANNOUNCE_LEADER 1
-#endif
-__device__ inline void help_announced(ring* q, const cfg& c, uint32_t ann, uint32_t tid) {
-    if (!GCQ_ANNOUNCE_LEADER) {
-        help_enqueue(q, c, &c.rec[ann - 1], tid);
-        return;
-    }
-    const unsigned m = __activemask();
-    if ((int)lane_id() == __ffs(m) - 1) {
-        help_enqueue(q, c, &c.rec[ann - 1], tid);
-        return;
-    }
-    uint32_t ns = 64;
-    for (int k = 0; k < 16 && ld_rlx(&q->Announce) == ann; ++k) {
-        __nanosleep(ns);
-        ns = ns < 1024 ? 2 * ns : ns;
-    }
-}
 template <bool Publish = true, bool HelpAfter = false>
 __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t first_raw = 0,
                                helper_state* hs = nullptr) {
@@ -494,17 +452,14 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
     if (tid >= c.max_threads) { raise_error(c.err, ERR_TID); return; }
     if (!HelpAfter) help_threads(q, c, tid, hs);
     uint64_t tail = 0;
-    uint32_t ann = 0;
     for (uint32_t count = c.enq_patience; --count != 0;) {
         if (first_raw) {
-            tail = try_enq_at<Publish>(q, c, index, c.counter(first_raw), &ann);
+            tail = try_enq_at<Publish>(q, c, index, c.counter(first_raw));
             first_raw = 0;
         } else {
-            tail = try_enq<Publish>(q, c, index, &ann);
+            tail = try_enq<Publish>(q, c, index);
         }
         if (tail == 0) {
-            if (GCQ_ANNOUNCE && ann != 0 && ann <= c.max_threads && ann - 1 != tid)
-                help_announced(q, c, ann, tid);
             if (HelpAfter) help_threads(q, c, tid, hs);
             return;
         }
@@ -519,9 +474,7 @@ __device__ inline void enqueue(ring* q, uint32_t index, uint32_t tid, uint64_t f
     st_rlx(&r->enqueue, 1u);
     st_rel(&r->seq2, seq);
     st_rel(&r->pending, 1u);
-    const bool announced = GCQ_ANNOUNCE && cas(&q->Announce, 0u, tid + 1) == 0u;
     enqueue_slow(q, c, tail_local, index, r, tid);
-    if (announced) cas(&q->Announce, tid + 1, 0u);
     st_rel(&r->pending, 0u);
     st_rel(&r->seq1, seq + 1);
     if (HelpAfter) help_threads(q, c, tid, hs);

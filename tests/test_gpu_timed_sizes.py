@@ -13,9 +13,7 @@ values:
   kernel's roles (gcq_fifo_check_split);
 * split-mode histories of 16384 threads through the oracle's O(n log n) pattern
   scan (sound: every pattern it reports is a violation; complete for the value
-  patterns when no dequeue reports empty);
-* bounded G-WFQ split runs at the sweep's largest sizes, where producers flood
-  the slow path, then the FIFO check.
+  patterns when no dequeue reports empty).
 """
 import numpy as np
 import pytest
@@ -87,19 +85,3 @@ def test_balanced_chunk_then_drain_conserves_payloads(gcq, kind, cap, threads):
         assert np.all(pos < len(vals)) and np.array_equal(vals[pos], lv)
         assert np.all(lc <= cnt[pos])
         assert q.error_word() == 0
-
-
-@pytest.mark.parametrize("threads,pct", [(65536, 25), (131072, 25), (262144, 50), (262144, 25)])
-def test_gwfq_split_producer_floods_complete(gcq, threads, pct):
-    """Split mode at capacity 2^20 with 10^4-10^5 producers: a producer that reaches
-    the wait-free slow path takes its tickets with a CAS on Tail that the other
-    producers' fast-path fetch-and-adds keep failing.  Its request is announced and
-    the fast-path enqueuers help it, so bounded runs at these sizes end with no
-    spin-bound error, keep making progress, and leave a queue that passes the FIFO
-    check."""
-    with gcq.Queue("gwfq", 20, threads) as q:
-        r = q.tb_run_bounded(1, threads, chunk_ops=128, producer_percent=pct, warmup_ms=20, run_ms=100)
-        assert q.error_word() == 0
-        assert r["enq_success"] > 0 and r["deq_success"] > 0
-        f = q.fifo_check(threads=threads, ops_per_thread=32)
-        assert f["verified"] == 1, f
