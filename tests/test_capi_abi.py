@@ -80,6 +80,14 @@ def test_argument_checks_without_gpu(built_lib):
     ctx = ctypes.c_void_p()
     assert L.gcq_rt_ctx_create(g.KINDS["sfq"], 1, 64, 64, 64, 32, 4, 10, 1, 0, ctypes.byref(ctx)) == g.ECAPACITY
     assert L.gcq_rt_ctx_render(None, None, 0, None, ctypes.byref(r)) == g.EINVAL
+    # harness checks and bounded runs: a null queue or a missing result is rejected
+    # before any device work
+    tr = g.TbResult()
+    assert L.gcq_tb_run_bounded(None, 0, 50, 1024, 256, 128, 10.0, 10.0, 0, ctypes.byref(tr)) == g.EINVAL
+    fr = g.FifoResult()
+    assert L.gcq_fifo_check_split(None, 1024, 256, 50, 32, ctypes.byref(fr)) == g.EINVAL
+    n = ctypes.c_size_t()
+    assert L.gcq_drain_host(None, 1024, 256, None, 0, ctypes.byref(n)) == g.EINVAL
     # served engine defaults
     cfg = g.ServeCfg()
     L.gcq_serve_default_cfg(ctypes.byref(cfg))
