@@ -87,7 +87,10 @@ int gcq_destroy(gcq_queue* q);
  * serial init, bfs_bench.cpp:531-552). */
 int gcq_reset(gcq_queue* q, void* stream);
 /* Device address of the queue object for kernels using the headers in include/gcq/:
- * gcq::gwf::mpmc*, gcq::glf::mpmc*, gcq::ymc::queue* or gcq::sfq::queue*. */
+ * gcq::gwf::mpmc*, gcq::glf::mpmc*, gcq::ymc::queue* or gcq::sfq::queue*.  As in the
+ * reference, a successful enqueue publishes the calling thread's earlier writes to
+ * the thread that dequeues the value (release on the enqueue, acquire on the
+ * dequeue, at gpu scope). */
 int gcq_device_ptr(gcq_queue* q, void** dev);
 /* Read (and optionally clear) the device error word; synchronises the device. */
 int gcq_error_word(gcq_queue* q, uint32_t* err, int clear);
