@@ -266,14 +266,34 @@ __device__ inline bool slow_faa(ring* q, const cfg& c, u64a* globalp, u64a* loca
         uint64_t gp = ld_acq(globalp);
         const uint32_t gt = c.thridx(gp);
         if (gt != (uint32_t)c.null_tid()) {
-            // help the phase-2 request named by the global word (gwf_ring.hpp:550-590)
+            // help the phase-2 request named by the global word (gwf_ring.hpp:550-590).
+            // A thread has one phase-2 record for both counters, and a counter word
+            // keeps a thread index after that thread's own clean-up CAS lost to a
+            // fetch-and-add, so the record read here may describe an increment of
+            // the other counter, or a later one of this counter whose CAS has not
+            // happened.  Clearing INC for it hands that thread a ticket the counter
+            // also gives to a fast-path operation: two enqueuers on one ticket lose
+            // a value, two dequeuers duplicate one (the reference clears it whenever
+            // the record's seqlock matches).  INC is cleared only when the record's
+            // local is fed by this counter and the word, read again after the
+            // record, still names the thread past the record's count -- true for the
+            // phase 2 of that thread's successful CAS until its index is cleaned,
+            // and the first cleaner clears INC before it cleans.
             record* hr = &c.rec[gt];
             const uint32_t seq = ld_acq(&hr->p2_seq2);
             u64a* p2_local = (u64a*)(uintptr_t)ld_rlx(&hr->p2_local);
             const uint64_t p2_cnt = ld_rlx(&hr->p2_cnt);
             fence_acq_rel();
-            const uint32_t seq1 = ld_rlx(&hr->p2_seq1);
-            if (seq1 == seq && p2_local) cas(p2_local, p2_cnt | local::INC, p2_cnt);
+            const uint32_t seq1 = ld_acq(&hr->p2_seq1);
+            bool help_ok = seq1 == seq && p2_local;
+            if (help_ok) {
+                const uint64_t g2 = ld_acq(globalp);
+                const uintptr_t base = (uintptr_t)(globalp == &q->Tail ? &c.rec[0].localTail : &c.rec[0].localHead);
+                const uintptr_t a = (uintptr_t)p2_local;
+                help_ok = a >= base && (a - base) % sizeof(record) == 0 && (a - base) / sizeof(record) < c.max_threads &&
+                          c.thridx(g2) == gt && c.counter(g2) > (p2_cnt >> 2);
+            }
+            if (help_ok) cas(p2_local, p2_cnt | local::INC, p2_cnt);
             const uint64_t clean = c.pack_global(c.counter(gp), c.null_tid());
             if (!cas_ok(globalp, gp, clean)) continue;
             gp = clean;

@@ -105,6 +105,10 @@ struct Ring {
     // true: gwf_ring.hpp:697-704 verbatim (a cycle match counts as produced even
     // when the slot was passed by a dequeuer); false: the corrected rule
     bool reference_produced_rule = false;
+    // true: gwf_ring.hpp:548-590 verbatim (a helper that finds a thread index in the
+    // counter word clears INC on that thread's phase-2 local whenever the record's
+    // seqlock matches); false: the checked form of slow_faa below
+    bool reference_phase2_help = false;
     std::unique_ptr<std::atomic<u64>[]> Entry;
     std::unique_ptr<Rec[]> Record;
 
@@ -253,7 +257,28 @@ struct Ring {
                 auto* p2l = (std::atomic<u64>*)(uintptr_t)hr.p2_local.load();
                 u64 p2c = hr.p2_cnt.load();
                 u32 s1 = hr.p2_seq1.load();
-                if (s1 == seq && p2l) {
+                // A thread has one phase-2 record for both counters, and a counter
+                // word keeps a thread index after that thread's own clean-up CAS
+                // lost to a fetch-and-add.  So the record read here may describe an
+                // increment of the other counter, or a later one of this counter
+                // whose CAS has not happened.  Clearing INC for it hands that
+                // thread a ticket the counter also gives to a fast-path operation:
+                // two enqueuers on one ticket lose a value, two dequeuers duplicate
+                // one.  The INC is cleared only when the record's local is fed by
+                // this counter and the word, read again after the record, still
+                // names the thread past the record's count -- which holds for the
+                // phase 2 of that thread's successful CAS until its thread index is
+                // cleaned, and the first cleaner clears INC before it cleans.
+                bool help_ok = s1 == seq && p2l;
+                if (help_ok && !reference_phase2_help) {
+                    const u64 g2 = gp_->load();
+                    const uintptr_t base = (gp_ == &Tail) ? (uintptr_t)&Record[0].localTail
+                                                          : (uintptr_t)&Record[0].localHead;
+                    const uintptr_t a = (uintptr_t)p2l;
+                    help_ok = a >= base && (a - base) % sizeof(Rec) == 0 && (a - base) / sizeof(Rec) < max_threads &&
+                              tid_of(g2) == gt && cnt_of(g2) > (p2c >> 2);
+                }
+                if (help_ok) {
                     u64 e = p2c | INC;
                     p2l->compare_exchange_strong(e, p2c);
                 }
@@ -1324,6 +1349,58 @@ int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_del
     stats[2] = worker_once;
     stats[3] = enqueued;
     return (ok && seen_while_stalled == 1 && stalled_total == 1 && worker_once == enqueued) ? 1 : 0;
+}
+
+// Exactly-once stress of G-WFQ's slow paths (the CPU port): `threads` threads each
+// run `ops` enqueue/dequeue pairs of their own values with the given patiences
+// (1: every operation starts on the slow path; 2: after one failed fast-path
+// attempt) and help delay, then the queue is drained.  Returns how many of `runs`
+// runs lost or duplicated a value.  reference_help = 1 runs the phase-2 help of
+// gwf_ring.hpp:548-590 verbatim.
+int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience, uint32_t deq_patience,
+                           uint32_t help_delay, uint32_t runs, int reference_help) {
+    if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || help_delay == 0 || runs == 0) return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        gwf::Ring q;
+        gwf::Knobs kn;
+        kn.help_delay = (int)help_delay;
+        kn.enq_patience = (int)enq_patience;
+        kn.deq_patience = (int)deq_patience;
+        q.init(1024, threads, bits_for(threads), kn);
+        q.reference_phase2_help = reference_help != 0;
+        std::vector<std::vector<u32>> got(threads);
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                for (u32 i = 0; i < ops; ++i) {
+                    q.enqueue_wf(1000 + w * ops + i, w);
+                    const u32 v = q.dequeue_wf(w);
+                    if (v != gwf::BOT) got[w].push_back(v);
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts((size_t)threads * ops, 0);
+        bool ok = true;
+        auto take = [&](u32 v) {
+            if (v < 1000 || v - 1000 >= threads * ops) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u32 v : g) take(v);
+        for (u32 k = 0; k < threads * ops + 16; ++k) {
+            const u32 v = q.dequeue_wf(0);
+            if (v == gwf::BOT) break;
+            take(v);
+        }
+        for (u32 c : counts) ok = ok && c == 1;
+        failed += ok ? 0 : 1;
+    }
+    return failed;
 }
 
 }  // extern "C"

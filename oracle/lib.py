@@ -82,6 +82,8 @@ _EXTRA = [
     ("oracle_levels_checksum", [C.c_int32, C.c_void_p], C.c_uint64),
     ("oracle_gwf_slow_passed_slot", [C.c_int, C.c_void_p], C.c_int),
     ("oracle_gwf_stalled_helping", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p], C.c_int),
+    ("oracle_gwf_slow_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int],
+     C.c_int),
 ]
 
 

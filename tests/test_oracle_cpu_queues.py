@@ -75,3 +75,17 @@ def test_gwf_stalled_request_control_without_helping(oracle_lib):
     assert oracle_lib.lib().oracle_gwf_stalled_helping(8, 64, 1 << 20, st.ctypes.data) == 0
     assert (int(st[0]), int(st[1])) == (0, 1)
     assert st[2] == st[3]
+
+
+@pytest.mark.parametrize("threads, ops, enq_patience, deq_patience, help_delay",
+                         [(8, 256, 1, 1, 1), (8, 256, 2, 2, 1 << 20), (8, 256, 1, 1 << 20, 1 << 20),
+                          (8, 256, 2, 2, 1), (32, 64, 1, 1, 1)])
+def test_gwf_slow_paths_exactly_once(oracle_lib, threads, ops, enq_patience, deq_patience, help_delay):
+    """Every operation on the slow path (patience 1), or after one failed fast-path
+    attempt (patience 2), with helping on every operation or never: each value comes
+    out exactly once in every run.  The phase-2 help of gwf_ring.hpp:548-590, run
+    verbatim, loses or duplicates values in some runs of these configurations (a
+    helper clears INC for a record that describes the other counter, or an
+    increment whose CAS has not happened); the port checks the record first."""
+    failed = oracle_lib.lib().oracle_gwf_slow_stress(threads, ops, enq_patience, deq_patience, help_delay, 60, 0)
+    assert failed == 0
