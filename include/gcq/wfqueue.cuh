@@ -167,7 +167,12 @@ __device__ inline bool enq_slow(const ctx& x, uint32_t hid, uint64_t v, uint64_t
     const uint64_t final_id = state_low(ld_acq(&h->enq_state));
     cell* d = x.find_cell(final_id);
     if (d) {
-        if (ld_acq(&d->val) == TOP) enq_commit(x, d, v, final_id);
+        // The value goes into the claimed cell before the enqueue returns, as in
+        // Yang & Mellor-Crummey's enq_slow.  wfqueue_hip_opt.hpp:313-314 commits only
+        // when the cell already reads TOP; a cell still at BOTTOM then waits for a
+        // dequeuer to commit the request's value, which this handle's next slow
+        // enqueue overwrites, and the value is lost.
+        enq_commit(x, d, v, final_id);
         return true;
     }
     return false;   // pool exhausted: the value was dropped, as in the reference
@@ -271,9 +276,17 @@ __device__ inline void help_deq(const ctx& x, uint32_t hid, uint32_t helpee) {
         const uint64_t aidx = state_low(s);
         cell* c = x.find_cell(aidx);
         if (!c) return;
-        const uint64_t cur_deq = ld_acq(&c->deq);
-        if (ld_acq(&c->val) == TOP || cas(&c->deq, REQ_NULL, x.req_of(helpee)) == REQ_NULL ||
-            cur_deq == x.req_of(helpee)) {
+        // Claimed for this request by this helper or by another one: the value the
+        // CAS found is compared, as Yang & Mellor-Crummey's help_deq does.
+        // wfqueue_hip_opt.hpp:489-492 compares a value loaded before the CAS, so a
+        // helper that loses the claim to another helper of the same request moves
+        // on, announces a later cell, and the claimed cell's value is orphaned.
+        bool claimed = ld_acq(&c->val) == TOP;
+        if (!claimed) {
+            const uint64_t prev = cas(&c->deq, REQ_NULL, x.req_of(helpee));
+            claimed = prev == REQ_NULL || prev == x.req_of(helpee);
+        }
+        if (claimed) {
             cas(&r->deq_state, s, pack_state(0, aidx));
             return;
         }

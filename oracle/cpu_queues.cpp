@@ -785,7 +785,12 @@ struct Queue {
         u64 fid = low(r.state.load());
         Cell* d = find_cell(fid);
         if (d) {
-            if (d->val.load() == TOP) enq_commit(d, v, fid);
+            // The value goes into the claimed cell before the enqueue returns, as in
+            // Yang & Mellor-Crummey's enq_slow.  wfqueue_hip_opt.hpp:313-314 commits
+            // only when the cell already reads TOP; a cell still at BOTTOM then waits
+            // for a dequeuer to commit the request's val, which this handle's next
+            // slow enqueue overwrites.
+            enq_commit(d, v, fid);
             return true;
         }
         return false;
@@ -891,10 +896,14 @@ struct Queue {
             u64 a = low(s);
             Cell* c = find_cell(a);
             if (!c) return;
-            u64 cur = c->deq.load();
+            // Claimed for this request by this helper or by another one: the value
+            // the CAS found is compared, as Yang & Mellor-Crummey's help_deq does.
+            // wfqueue_hip_opt.hpp:489-492 compares a value loaded before the CAS, so
+            // a helper that loses the claim to another helper of the same request
+            // moves on, announces a later cell, and the claimed cell is orphaned.
             u64 e = NUL;
             if (c->val.load() == TOP || c->deq.compare_exchange_strong(e, (u64)(uintptr_t)&r) ||
-                cur == (u64)(uintptr_t)&r) {
+                e == (u64)(uintptr_t)&r) {
                 u64 se = s;
                 r.state.compare_exchange_strong(se, pst(0, a));
                 return;
@@ -1395,6 +1404,51 @@ int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience
         for (u32 k = 0; k < threads * ops + 16; ++k) {
             const u32 v = q.dequeue_wf(0);
             if (v == gwf::BOT) break;
+            take(v);
+        }
+        for (u32 c : counts) ok = ok && c == 1;
+        failed += ok ? 0 : 1;
+    }
+    return failed;
+}
+
+// Exactly-once stress of the YMC port: `threads` threads each run `ops`
+// enqueue/dequeue pairs of their own values with the given patience (0: one
+// fast-path attempt, then the slow path), then the queue is drained.  Returns how
+// many of `runs` runs lost or duplicated a value.
+int oracle_ymc_slow_stress(uint32_t threads, uint32_t ops, int patience, uint32_t runs) {
+    if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || patience < 0 || runs == 0) return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        ymc::Queue q;
+        q.init((int)threads, (int)ops);
+        q.patience = patience;
+        std::vector<std::vector<u64>> got(threads);
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                for (u32 i = 0; i < ops; ++i) {
+                    q.enqueue(1000 + (u64)w * ops + i, (int)w);
+                    const u64 v = q.dequeue((int)w);
+                    if (v != ymc::EMPTY) got[w].push_back(v);
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts((size_t)threads * ops, 0);
+        bool ok = true;
+        auto take = [&](u64 v) {
+            if (v < 1000 || v - 1000 >= (u64)threads * ops) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u64 v : g) take(v);
+        for (u32 k = 0; k < threads * ops + 16; ++k) {
+            const u64 v = q.dequeue(0);
+            if (v == ymc::EMPTY) break;
             take(v);
         }
         for (u32 c : counts) ok = ok && c == 1;

@@ -84,6 +84,7 @@ _EXTRA = [
     ("oracle_gwf_stalled_helping", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p], C.c_int),
     ("oracle_gwf_slow_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int],
      C.c_int),
+    ("oracle_ymc_slow_stress", [C.c_uint32, C.c_uint32, C.c_int, C.c_uint32], C.c_int),
 ]
 
 
