@@ -268,8 +268,13 @@ __device__ inline void help_deq(const ctx& x, uint32_t hid, uint32_t helpee) {
             if (!state_pending(s) || ld_rlx(&r->deq_id) != id) return;
         }
         if (cand) {
-            cas(&r->deq_state, pack_state(1, prior), pack_state(1, cand));
-            cand = 0;
+            // The candidate is kept when a smaller cell is announced instead: that cell
+            // is tried first, and if its claim fails this one is announced next (Yang &
+            // Mellor-Crummey's "if (idx >= new) new = 0").  Dropping it, as
+            // wfqueue_hip_opt.hpp:474-479 does, resumes the scan past it, and its value
+            // is left behind the request's cell.
+            const uint64_t seen = cas(&r->deq_state, pack_state(1, prior), pack_state(1, cand));
+            if (seen == pack_state(1, prior) || !state_pending(seen) || state_low(seen) >= cand) cand = 0;
         }
         s = ld_acq(&r->deq_state);
         if (!state_pending(s) || ld_rlx(&r->deq_id) != id) return;

@@ -887,9 +887,13 @@ struct Queue {
                 if (!pend(s) || r.id.load() != id) return;
             }
             if (cand) {
+                // The candidate is kept when a smaller cell is announced instead: that
+                // cell is tried first, and if its claim fails this one is announced
+                // next (Yang & Mellor-Crummey's "if (idx >= new) new = 0").  Dropping
+                // it, as wfqueue_hip_opt.hpp:474-479 does, resumes the scan past it,
+                // and its value is left behind the request's cell.
                 u64 e = pst(1, prior);
-                r.state.compare_exchange_strong(e, pst(1, cand));
-                cand = 0;
+                if (r.state.compare_exchange_strong(e, pst(1, cand)) || !pend(e) || low(e) >= cand) cand = 0;
             }
             s = r.state.load();
             if (!pend(s) || r.id.load() != id) return;
