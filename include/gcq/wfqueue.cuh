@@ -226,7 +226,11 @@ __device__ inline uint64_t help_enq(const ctx& x, uint32_t hid, cell* c, uint64_
             if (ld_acq(&c->val) == TOP) enq_commit(x, c, v, i);
             return ld_acq(&c->val);
         }
-        return ld_acq(&x.q->T) <= i ? EMPTY : RETRY;
+        // Bound to a request that took another cell: the cell is dead (TOP), not
+        // evidence of an empty queue, as in Yang & Mellor-Crummey's help_enq.
+        // wfqueue_hip_opt.hpp:394-395 returns EMPTY here when T <= i, which lets a
+        // dequeue request complete empty at this cell past a value cell behind it.
+        return ld_acq(&c->val);
     }
     if (rid > i) return ld_acq(&x.q->T) <= i ? EMPTY : RETRY;
     if (try_to_claim_req(&rh->enq_state, rid, i) || ld_acq(&rh->enq_state) == pack_state(0, i)) {

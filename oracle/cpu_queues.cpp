@@ -847,7 +847,10 @@ struct Queue {
                 if (c->val.load() == TOP) enq_commit(c, v, i);
                 return c->val.load();
             }
-            return T.load() <= i ? EMPTY : RETRY;
+            // bound to a request that took another cell: the cell is dead (TOP), not
+            // evidence of an empty queue, as in Yang & Mellor-Crummey's help_enq;
+            // wfqueue_hip_opt.hpp:394-395 returns EMPTY here when T <= i
+            return c->val.load();
         }
         if (rid > i) return T.load() <= i ? EMPTY : RETRY;
         if (claim(r->state, rid, i) || r->state.load() == pst(0, i)) {

@@ -91,15 +91,16 @@ def test_gwf_slow_paths_exactly_once(oracle_lib, threads, ops, enq_patience, deq
     assert failed == 0
 
 
-@pytest.mark.parametrize("threads, ops, patience", [(8, 256, 1), (8, 256, 2), (32, 64, 1), (8, 256, 16)])
+@pytest.mark.parametrize("threads, ops, patience", [(8, 256, 0), (64, 32, 0), (8, 256, 1), (32, 64, 1), (8, 256, 16)])
 def test_ymc_slow_paths_exactly_once(oracle_lib, threads, ops, patience):
     """YMC with one or two fast-path attempts before the slow path, and with the
-    default patience: each value comes out exactly once in every run.  Three
+    default patience: each value comes out exactly once in every run.  Four
     departures from wfqueue_hip_opt.hpp restore Yang & Mellor-Crummey's rules: the
     slow enqueue writes its value into the claimed cell before it returns (:313-314
     writes it only into a cell already at TOP), a dequeue helper treats a cell as
     claimed for its request by the value its CAS found (:489-492 compares a value
-    loaded before the CAS), and a helper keeps its candidate cell when a smaller one
-    is announced instead (:474-479 drops it).  With patience 0 a rarer loss remains
-    (about one run in 10^4), not covered here."""
-    assert oracle_lib.lib().oracle_ymc_slow_stress(threads, ops, patience, 100) == 0
+    loaded before the CAS), a helper keeps its candidate cell when a smaller one is
+    announced instead (:474-479 drops it), and a cell bound to a request that took
+    another cell is dead, not empty (:394-395 returns EMPTY when T <= i).  With only
+    the first three, about one run in 10^4 at patience 0 still lost a value."""
+    assert oracle_lib.lib().oracle_ymc_slow_stress(threads, ops, patience, 150) == 0
