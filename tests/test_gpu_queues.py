@@ -86,6 +86,22 @@ def test_gwfq_slow_path_and_helping(gcq, oracle_lib):
         assert q.error_word() == 0
 
 
+def test_ymc_slow_path_and_helping(gcq, oracle_lib):
+    """Patience 0 sends every YMC operation that misses its first cell to the slow
+    path (enqueue requests bound to cells by dequeuers, dequeue requests announced
+    and claimed by helpers): histories check linearizable and a produce-then-drain
+    FIFO check takes every token exactly once."""
+    with gcq.Queue("wfq", 0, 1024, ymc_patience=0) as q:
+        for rep in range(3):
+            recs = q.history(threads=128, ops=32, block=128)
+            _lin(oracle_lib, recs)
+            recs = q.history(threads=32, ops=16, block=32, mode=1, producer_percent=50)
+            _lin(oracle_lib, recs)
+        r = q.fifo_check(threads=1024, ops_per_thread=32)
+        assert r["verified"] == 1, r
+        assert q.error_word() & ~gcq.ERR_POOL == 0
+
+
 def test_gwfq_remap_layout(gcq, oracle_lib):
     with gcq.Queue("gwfq", 10, 256, remap=1) as q:
         recs = q.history(threads=256, ops=16, block=256)
