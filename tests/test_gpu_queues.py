@@ -103,7 +103,7 @@ def test_ymc_slow_path_and_helping(gcq, oracle_lib):
             _lin(oracle_lib, recs)
             recs = q.history(threads=32, ops=16, block=32, mode=1, producer_percent=50)
             _lin(oracle_lib, recs)
-        r = q.fifo_check(threads=1024, ops_per_thread=32)
+        r = q.fifo_check(threads=256, ops_per_thread=32)
         assert r["verified"] == 1, r
         assert q.error_word() & ~gcq.ERR_POOL == 0
 
