@@ -159,6 +159,11 @@ __device__ __forceinline__ uint64_t try_enq(ring* q, const cfg& c, uint32_t inde
 // dequeuer holding the same ticket would mark it, so that dequeuer does not wait
 // for an index that will not come.  A slot holding an older index is left for that
 // dequeuer.  Not waited for; a failed CAS means the slot moved on and needs nothing.
+// The dequeuer that reaches the ticket fails there and spends one unit of Threshold
+// with no element behind it, a failure SCQ's 3n - 1 bound does not count; the
+// abandoning thread resets Threshold, as an enqueue does, so the bound still holds
+// from there on (callers also take such tickets at most once per thread between two
+// successful enqueues, see enqueue_ptr).
 __device__ inline void abandon_enq_ticket(ring* q, uint64_t T_raw) {
     const cfg c = load_cfg(q);
     const uint64_t T = c.counter(T_raw);
@@ -167,6 +172,7 @@ __device__ inline void abandon_enq_ticket(ring* q, uint64_t T_raw) {
     const uint64_t E = ld_rlx(&c.entry[j]);
     if (cycle_cmp(entry::cycle(E), tcyc) < 0 && entry::empty_index(entry::index(E)))
         cas_rlx(&c.entry[j], E, entry::pack(entry::note(E), tcyc, entry::safe(E), true, BOT));
+    reset_threshold(&q->Threshold, c.threshold_max());
 }
 
 // try_deq, gwf_ring.hpp:421-472.  0 when finished (*out = index, or BOT if the
@@ -183,9 +189,9 @@ __device__ inline uint64_t try_deq(ring* q, const cfg& c, uint32_t* out, uint32_
     const uint32_t hcyc = c.cycle_of(H);
     const uint32_t j = c.slot_of(H);
     ticket_req pf;
-    if (PF) pf = ticket_issue(pf_ctr, c.cinc());
+    if (PF && pf_ctr) pf = ticket_issue(pf_ctr, c.cinc());
     uint64_t E = ld_acq(&c.entry[j]);   // acquire: see consume
-    if (PF) *pf_raw = ticket_take(pf, c.cinc());
+    if (PF && pf_ctr) *pf_raw = ticket_take(pf, c.cinc());
     // The slot of an earlier cycle with no index: the enqueuer holding this ticket
     // may be about to fill it.  Marking it now would make that enqueuer retry with a
     // new ticket, and this dequeuer too; re-reading it a few times first (bounded,
@@ -682,8 +688,17 @@ __device__ __forceinline__ void ctx_store(const mpmc_view& q, uint32_t tid, cons
 __device__ __forceinline__ bool enqueue_ptr(const mpmc_view& q, uint64_t value, uint32_t tid,
                                             thread_ctx* x = nullptr) {
 #if GCQ_TICKET_PREFETCH
+    // The aq ticket is taken ahead of need only by a thread with a context whose last
+    // free-ring dequeue succeeded.  A ticket taken for an operation that then finds
+    // the queue full is abandoned; a thread that kept prefetching while the queue
+    // stayed full would drive Tail ahead of the elements by one abandoned ticket per
+    // attempt, the dequeuers failing on them would spend Threshold below zero, and
+    // dequeues would report a full queue empty (a CPU model of this path lost values
+    // that way).  So a thread abandons at most one ticket between two successful
+    // enqueues, and callers without a context take no aq ticket ahead of need.
     uint64_t aq_raw = 0;
-    const uint32_t idx = dequeue<true>(q.fq, tid, &q.aq->Tail, &aq_raw, x ? &x->help_fq : nullptr,
+    const bool pf = x && !x->fq_empty;
+    const uint32_t idx = dequeue<true>(q.fq, tid, pf ? &q.aq->Tail : nullptr, &aq_raw, x ? &x->help_fq : nullptr,
                                        x && x->fq_fresh, x && x->fq_empty);
     if (x) {
         x->fq_fresh = false;
