@@ -1023,6 +1023,144 @@ static inline bool q_dequeue(AnyQueue* q, u64* out, u32 tid, bool split) {
     }
 }
 
+
+// -----------------------------------------------------------------------------
+// Model of the device G-WFQ MPMC path (test infrastructure).  The device
+// Enqueue_Ptr / Dequeue_Ptr add to the reference's algorithm: the second ring's
+// ticket taken beside the first ring's access (an aq ticket that an Enqueue_Ptr
+// finding the queue full abandons), the empty exit before a ticket (with catchup),
+// and a per-thread context that skips the Threshold pre-check after the thread's
+// own enqueue and tries the empty exit first after its own empty dequeue.  This
+// restates those additions over the rings above so that a stress on the CPU can
+// check them for exactly-once delivery.  prefetch: 0 none, 1 an aq ticket on every
+// Enqueue_Ptr, 2 only while the thread's last free-ring dequeue succeeded, with a
+// Threshold reset when a ticket is abandoned (the device's rule).
+namespace gwfmodel {
+using namespace gwf;
+struct Ctx { bool aq_fresh = false, fq_fresh = false, aq_empty = false, fq_empty = false; };
+static bool seen_empty(Ring& q) {
+    const u64 h = q.cnt_of(q.Head.load());
+    const u64 t = q.cnt_of(q.Tail.load());
+    if (t > h) return false;
+    if (t < h) q.catchup(t, h);
+    return true;
+}
+static u64 try_enq_at(Ring& q, u32 index, u64 T) {
+    const u32 tc = q.cycle_of(T), j = q.slot_of(T);
+    u64 E = q.Entry[j].load();
+    for (;;) {
+        const u32 ec = cyc(E), ei = idx(E);
+        if (ccmp(ec, tc) < 0 && (safe(E) || q.cnt_of(q.Head.load()) <= T) && (ei == BOT || ei == BOT_C)) {
+            if (!q.Entry[j].compare_exchange_strong(E, pack(note(E), tc, true, true, index))) continue;
+            if (q.Threshold.load() != q.thr_max()) q.Threshold.exchange(q.thr_max());
+            return 0;
+        }
+        return T;
+    }
+}
+static u64 try_deq_pf(Ring& q, u32* out, u32 me, std::atomic<u64>* pf, u64* pf_raw) {
+    const u64 H = q.cnt_of(q.Head.fetch_add(q.cinc));
+    if (pf) *pf_raw = pf->fetch_add(q.cinc);
+    const u32 hc = q.cycle_of(H), j = q.slot_of(H);
+    u64 E = q.Entry[j].load();
+    for (;;) {
+        const u32 ec = cyc(E), ei = idx(E);
+        if (ccmp(ec, hc) == 0 && ei != BOT && ei != BOT_C) { q.consume(H, j, E, me); *out = ei; return 0; }
+        if (ccmp(ec, hc) >= 0) break;
+        const u64 nw = (ei == BOT || ei == BOT_C) ? pack(note(E), hc, safe(E), true, BOT)
+                                                  : pack(note(E), ec, false, enq(E), ei);
+        if (q.Entry[j].compare_exchange_strong(E, nw)) break;
+    }
+    const u64 T = q.cnt_of(q.Tail.load());
+    if (T <= H + 1) { q.catchup(T, H + 1); q.Threshold.fetch_sub(1); *out = BOT; return 0; }
+    if (q.Threshold.fetch_sub(1) <= 0) { *out = BOT; return 0; }
+    return H;
+}
+static u32 dequeue(Ring& q, u32 me, std::atomic<u64>* pf, u64* pf_raw, bool skip_check, bool first_check) {
+    if (!skip_check && q.Threshold.load() < 0) return BOT;
+    if (first_check && seen_empty(q)) return BOT;
+    q.help_threads(me);
+    u32 out = BOT;
+    u64 head = 0;
+    if (pf) {
+        head = try_deq_pf(q, &out, me, pf, pf_raw);
+        if (head == 0) return out;
+        if (seen_empty(q)) return BOT;
+    }
+    for (int count = q.k.deq_patience - (pf ? 1 : 0); --count > 0;) {
+        head = try_deq_pf(q, &out, me, nullptr, nullptr);
+        if (head == 0) return out;
+        if (seen_empty(q)) return BOT;
+    }
+    Rec& r = q.Record[me];
+    const u32 seq = r.seq1.load();
+    r.localHead.store(head << 2); r.initHead.store(head << 2); r.enqueue.store(0);
+    r.seq2.store(seq); r.pending.store(1);
+    q.dequeue_slow(head << 2, r, me);
+    r.pending.store(0); r.seq1.store(seq + 1);
+    const u64 hr = r.localHead.load() >> 2;
+    const u32 j = q.slot_of(hr);
+    const u64 E = q.Entry[j].load();
+    if (ccmp(cyc(E), q.cycle_of(hr)) == 0 && idx(E) != BOT && idx(E) != BOT_C) { q.consume(hr, j, E, me); return idx(E); }
+    return BOT;
+}
+static void enqueue(Ring& q, u32 index, u32 me, u64 first_raw) {
+    q.help_threads(me);
+    u64 tail = 0;
+    for (int count = q.k.enq_patience; --count > 0;) {
+        const u64 T = first_raw ? q.cnt_of(first_raw) : q.cnt_of(q.Tail.fetch_add(q.cinc));
+        first_raw = 0;
+        tail = try_enq_at(q, index, T);
+        if (tail == 0) return;
+    }
+    if (first_raw) tail = q.cnt_of(first_raw);
+    Rec& r = q.Record[me];
+    const u32 seq = r.seq1.load();
+    r.localTail.store(tail << 2); r.initTail.store(tail << 2); r.index.store(index); r.enqueue.store(1);
+    r.seq2.store(seq); r.pending.store(1);
+    q.enqueue_slow(tail << 2, index, r, me);
+    r.pending.store(0); r.seq1.store(seq + 1);
+}
+static void abandon(Ring& q, u64 T_raw, bool reset) {
+    const u64 T = q.cnt_of(T_raw);
+    const u32 tc = q.cycle_of(T), j = q.slot_of(T);
+    u64 E = q.Entry[j].load();
+    if (ccmp(cyc(E), tc) < 0 && (idx(E) == BOT || idx(E) == BOT_C))
+        q.Entry[j].compare_exchange_strong(E, pack(note(E), tc, safe(E), true, BOT));
+    if (reset && q.Threshold.load() != q.thr_max()) q.Threshold.exchange(q.thr_max());
+}
+struct Queue {
+    Mpmc m;
+    int prefetch = 2;
+    bool enqueue_ptr(u64 v, u32 me, Ctx& x) {
+        u64 aq_raw = 0;
+        const bool pf = prefetch == 1 || (prefetch == 2 && !x.fq_empty);
+        const u32 i = dequeue(m.fq, me, pf ? &m.aq.Tail : nullptr, &aq_raw, x.fq_fresh, x.fq_empty);
+        x.fq_fresh = false;
+        x.fq_empty = (i == BOT);
+        if (i == BOT) {
+            if (aq_raw) abandon(m.aq, aq_raw, prefetch == 2);
+            return false;
+        }
+        m.data[i].store(v);
+        enqueue(m.aq, i, me, aq_raw);
+        x.aq_fresh = true;
+        return true;
+    }
+    bool dequeue_ptr(u64* out, u32 me, Ctx& x) {
+        const u32 i = dequeue(m.aq, me, nullptr, nullptr, x.aq_fresh, x.aq_empty);
+        x.aq_fresh = false;
+        x.aq_empty = (i == BOT);
+        if (i == BOT) return false;
+        const u64 fq_raw = m.fq.Tail.fetch_add(m.fq.cinc);
+        *out = m.data[i].load();
+        enqueue(m.fq, i, me, fq_raw);
+        x.fq_fresh = true;
+        return true;
+    }
+};
+}  // namespace gwfmodel
+
 }  // namespace
 
 extern "C" {
@@ -1459,6 +1597,68 @@ int oracle_ymc_slow_stress(uint32_t threads, uint32_t ops, int patience, uint32_
             take(v);
         }
         for (u32 c : counts) ok = ok && c == 1;
+        failed += ok ? 0 : 1;
+    }
+    return failed;
+}
+
+// Exactly-once stress of the device-path model (gwfmodel above): `threads` threads
+// run `ops` iterations in balanced mode (mode 0: enqueue then dequeue) or split
+// mode (mode 1: the first producer_percent % of threads enqueue, the rest
+// dequeue) on a ring of n entries, then the queue is drained.  Returns how many of
+// `runs` runs lost, duplicated or invented a value.
+int oracle_gwf_device_model_stress(uint32_t threads, uint32_t ops, uint32_t n, uint32_t enq_patience,
+                                   uint32_t deq_patience, uint32_t help_delay, int mode, int producer_percent,
+                                   int prefetch, uint32_t runs) {
+    if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || n < 2 || (n & (n - 1)) || n < threads ||
+        help_delay == 0 || runs == 0 || prefetch < 0 || prefetch > 2)
+        return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        gwfmodel::Queue d;
+        d.prefetch = prefetch;
+        gwf::Knobs k;
+        k.enq_patience = (int)enq_patience;
+        k.deq_patience = (int)deq_patience;
+        k.help_delay = (int)help_delay;
+        d.m.init(n, threads, bits_for(threads), k);
+        std::vector<std::vector<u64>> got(threads), put(threads);
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                gwfmodel::Ctx x;
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                const bool producer = (u64)w * 100 / threads < (u64)producer_percent;
+                for (u32 i = 0; i < ops; ++i) {
+                    const u64 v = 1000 + (u64)w * ops + i;
+                    u64 o;
+                    if (mode == 0 || producer)
+                        if (d.enqueue_ptr(v, w, x)) put[w].push_back(v);
+                    if (mode == 0 || !producer)
+                        if (d.dequeue_ptr(&o, w, x)) got[w].push_back(o);
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts((size_t)threads * ops, 0), in((size_t)threads * ops, 0);
+        for (auto& p : put)
+            for (u64 v : p) in[v - 1000] = 1;
+        bool ok = true;
+        auto take = [&](u64 v) {
+            if (v < 1000 || v - 1000 >= (u64)threads * ops || !in[v - 1000]) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u64 v : g) take(v);
+        gwfmodel::Ctx x;
+        u64 o;
+        for (u32 misses = 0, k2 = 0; k2 < threads * ops + 64 && misses < 64; ++k2) {
+            if (d.dequeue_ptr(&o, 0, x)) take(o);
+            else ++misses;
+        }
+        for (size_t i = 0; i < counts.size(); ++i) ok = ok && counts[i] == in[i];
         failed += ok ? 0 : 1;
     }
     return failed;

@@ -104,3 +104,21 @@ def test_ymc_slow_paths_exactly_once(oracle_lib, threads, ops, patience):
     another cell is dead, not empty (:394-395 returns EMPTY when T <= i).  With only
     the first three, about one run in 10^4 at patience 0 still lost a value."""
     assert oracle_lib.lib().oracle_ymc_slow_stress(threads, ops, patience, 150) == 0
+
+
+@pytest.mark.parametrize("threads, ops, n, patience, help_delay, mode, pct",
+                         [(16, 128, 32, 3, 2, 1, 75), (16, 128, 32, 0, 64, 1, 75), (8, 256, 16, 0, 64, 1, 50),
+                          (32, 64, 32, 0, 64, 1, 90), (8, 256, 64, 0, 64, 0, 50)])
+def test_gwf_device_path_model_exactly_once(oracle_lib, threads, ops, n, patience, help_delay, mode, pct):
+    """The device Enqueue_Ptr/Dequeue_Ptr additions (the second ring's ticket taken
+    beside the first ring's access, abandoned when the queue is full; the empty exit;
+    the per-thread context), restated over the CPU rings: with the device's rule --
+    an aq ticket taken ahead of need only while the thread's last free-ring dequeue
+    succeeded, and a Threshold reset when one is abandoned -- every value comes out
+    exactly once on small rings that fill.  (Taking the ticket on every attempt lost
+    values in some runs of these configurations: the abandoned tickets drove
+    Threshold below zero while the queue was full.)  patience 0 means the default
+    128 / 256."""
+    pe, pd = (patience, patience) if patience else (128, 256)
+    failed = oracle_lib.lib().oracle_gwf_device_model_stress(threads, ops, n, pe, pd, help_delay, mode, pct, 2, 300)
+    assert failed == 0
