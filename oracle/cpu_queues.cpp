@@ -22,10 +22,19 @@
 //   SFQ    sfqueue_hip.hpp:13-66 (layout, ids), sfqueue_hip.cpp:31-128 (ops),
 //          :134-144 (u64 wrapper)
 //
+// Where the reference's slow paths lose or duplicate values, the G-WFQ and YMC
+// restatements follow the published algorithms (each departure is marked where it
+// is made, and G-WFQ keeps flags that restore the reference's rules).
+//
 // Runners at the end drive them like the reference harnesses:
 //   history      correctness/history.cpp:188-227 with the logical clock of
 //                correctness/wf_linlog.hpp:25-45
 //   throughput   throughout_bench.cpp:810-882 (balanced and split kernels)
+// and stress them for exactly-once delivery (oracle_gwf_slow_stress,
+// oracle_ymc_slow_stress).  gwfmodel, before the runners, restates the device
+// MPMC path's additions to the reference algorithm for the same kind of stress
+// (oracle_gwf_device_model_stress); it is a model of the device code, not of the
+// reference.
 
 #include <algorithm>
 #include <atomic>
