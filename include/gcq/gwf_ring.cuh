@@ -378,8 +378,8 @@ __device__ inline bool try_deq_slow(ring* q, const cfg& c, uint64_t H_raw, recor
         const uint32_t ecyc = entry::cycle(P), enote = entry::note(P), eidx = entry::index(P);
         if (cycle_cmp(ecyc, hcyc) == 0 && !entry::empty_index(eidx)) {
             const uint64_t H_local = H_raw << 2;
-            cas(&r->localHead, H_local, H_local | local::FIN);
-            return true;
+            const uint64_t prev = cas(&r->localHead, H_local, H_local | local::FIN);
+            return prev == H_local || (prev & local::FIN) != 0;
         }
         uint32_t n_note = enote;
         uint64_t val = entry::pack(n_note, hcyc, entry::safe(P), true, BOT);
@@ -399,10 +399,15 @@ __device__ inline bool try_deq_slow(ring* q, const cfg& c, uint64_t H_raw, recor
     dekker_fence();
     const uint64_t T = c.counter(ld_acq(&q->Tail));
     if (T <= H_raw + 1) catchup(q, c, T, H_raw + 1);
+    // Done only when the request is finished: at this ticket (this CAS) or already
+    // (FIN).  gwf_ring.hpp:763-766 reports done whatever the CAS found; when another
+    // helper has moved the request to a later ticket, the owner then stops and
+    // gathers at that unfinished ticket (empty), and the helper that finishes the
+    // request there later claims an element nobody returns.
     if (ld_acq(&q->Threshold) < 0) {
         const uint64_t H_local = H_raw << 2;
-        cas(&r->localHead, H_local, H_local | local::FIN);
-        return true;
+        const uint64_t prev = cas(&r->localHead, H_local, H_local | local::FIN);
+        return prev == H_local || (prev & local::FIN) != 0;
     }
     return false;
 }

@@ -118,6 +118,9 @@ struct Ring {
     // counter word clears INC on that thread's phase-2 local whenever the record's
     // seqlock matches); false: the checked form of slow_faa below
     bool reference_phase2_help = false;
+    // true: gwf_ring.hpp:729-731, 763-766 verbatim (a slow dequeue attempt reports
+    // the request done whatever its FIN CAS found); false: done only once FIN is set
+    bool reference_finish_rule = false;
     std::unique_ptr<std::atomic<u64>[]> Entry;
     std::unique_ptr<Rec[]> Record;
 
@@ -357,8 +360,8 @@ struct Ring {
             u32 ec = cyc(P), en = note(P), ei = idx(P);
             if (ccmp(ec, hc) == 0 && ei != BOT && ei != BOT_C) {
                 u64 hl = H << 2;
-                r.localHead.compare_exchange_strong(hl, (H << 2) | FIN);
-                return true;
+                if (r.localHead.compare_exchange_strong(hl, (H << 2) | FIN) || reference_finish_rule) return true;
+                return (hl & FIN) != 0;
             }
             u32 nnote = en;
             u64 val = pack(nnote, hc, safe(P), true, BOT);
@@ -377,10 +380,15 @@ struct Ring {
         }
         u64 T = cnt_of(Tail.load());
         if (T <= H + 1) catchup(T, H + 1);
+        // Done only when the request is finished: at this ticket (this CAS) or
+        // already (FIN).  gwf_ring.hpp:763-766 reports done whatever the CAS found;
+        // when another helper has moved the request to a later ticket, the owner
+        // then stops and gathers at that unfinished ticket (empty), and the helper
+        // that finishes the request there later claims an element nobody returns.
         if (Threshold.load() < 0) {
             u64 hl = H << 2;
-            r.localHead.compare_exchange_strong(hl, (H << 2) | FIN);
-            return true;
+            if (r.localHead.compare_exchange_strong(hl, (H << 2) | FIN) || reference_finish_rule) return true;
+            return (hl & FIN) != 0;
         }
         return false;
     }
@@ -1559,6 +1567,70 @@ int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience
             const u32 v = q.dequeue_wf(0);
             if (v == gwf::BOT) break;
             take(v);
+        }
+        for (u32 c : counts) ok = ok && c == 1;
+        failed += ok ? 0 : 1;
+    }
+    return failed;
+}
+
+// Split-role stress of the G-WFQ port's single ring: P producer threads enqueue K
+// values each (P * K <= n, so the ring never overfills), C consumer threads dequeue
+// until every value came out or a 2 s bound passes; then the ring is drained.
+// Returns how many of `runs` runs lost, duplicated or invented a value.
+// reference_finish = 1 runs the slow dequeue's completion rule of
+// gwf_ring.hpp:729-731, 763-766 verbatim.
+int oracle_gwf_split_stress(uint32_t P, uint32_t Cn, uint32_t K, uint32_t n, uint32_t enq_patience,
+                            uint32_t deq_patience, uint32_t help_delay, uint32_t runs, int reference_finish) {
+    const uint32_t threads = P + Cn;
+    if (P == 0 || Cn == 0 || threads > 64 || K == 0 || (uint64_t)P * K > n || n < threads || (n & (n - 1)) ||
+        help_delay == 0 || runs == 0)
+        return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        gwf::Ring q;
+        gwf::Knobs kn;
+        kn.help_delay = (int)help_delay;
+        kn.enq_patience = (int)enq_patience;
+        kn.deq_patience = (int)deq_patience;
+        q.init(n, threads, bits_for(threads), kn);
+        q.reference_finish_rule = reference_finish != 0;
+        const u32 total = P * K;
+        std::vector<std::vector<u32>> got(threads);
+        std::atomic<u32> taken{0};
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        const auto deadline = std::chrono::steady_clock::now() + std::chrono::seconds(2);
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                if (w < P) {
+                    for (u32 i = 0; i < K; ++i) q.enqueue_wf(1000 + w * K + i, w);
+                    return;
+                }
+                while (taken.load() < total && std::chrono::steady_clock::now() < deadline) {
+                    const u32 v = q.dequeue_wf(w);
+                    if (v != gwf::BOT) {
+                        got[w].push_back(v);
+                        taken.fetch_add(1);
+                    }
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts(total, 0);
+        bool ok = true;
+        auto take = [&](u32 v) {
+            if (v < 1000 || v - 1000 >= total) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u32 v : g) take(v);
+        for (u32 misses = 0, k = 0; k < total + 64 && misses < 64; ++k) {
+            const u32 v = q.dequeue_wf(0);
+            if (v == gwf::BOT) ++misses;
+            else take(v);
         }
         for (u32 c : counts) ok = ok && c == 1;
         failed += ok ? 0 : 1;

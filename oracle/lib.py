@@ -85,6 +85,8 @@ _EXTRA = [
     ("oracle_gwf_slow_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int],
      C.c_int),
     ("oracle_ymc_slow_stress", [C.c_uint32, C.c_uint32, C.c_int, C.c_uint32], C.c_int),
+    ("oracle_gwf_split_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                 C.c_uint32, C.c_int], C.c_int),
     ("oracle_gwf_device_model_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                         C.c_int, C.c_int, C.c_int, C.c_uint32], C.c_int),
 ]

@@ -122,3 +122,15 @@ def test_gwf_device_path_model_exactly_once(oracle_lib, threads, ops, n, patienc
     pe, pd = (patience, patience) if patience else (128, 256)
     failed = oracle_lib.lib().oracle_gwf_device_model_stress(threads, ops, n, pe, pd, help_delay, mode, pct, 2, 300)
     assert failed == 0
+
+
+@pytest.mark.parametrize("P, C, K, n", [(4, 12, 4, 16), (8, 24, 8, 64), (8, 8, 8, 64), (16, 16, 4, 64)])
+def test_gwf_split_small_ring_exactly_once(oracle_lib, P, C, K, n):
+    """Split roles on one ring of 16-64 entries with patience 2 and a help delay of
+    1, so dequeues reach the slow path and help each other: every value comes out
+    exactly once.  A slow dequeue attempt that found Threshold below zero reports
+    the request done only once FIN is set; gwf_ring.hpp:763-766 reports it done
+    whatever its CAS found, and when another helper had moved the request to a later
+    ticket the owner returned empty while that helper later claimed an element for
+    it (0.2-0.35 % of runs lost a value)."""
+    assert oracle_lib.lib().oracle_gwf_split_stress(P, C, K, n, 2, 2, 1, 400, 0) == 0
