@@ -1,11 +1,15 @@
 // G-LFQ for sm_103a: the lock-free SCQ queue of glf_queue.hpp with
-// warp-aggregated tickets, 64-bit entries {Cycle8, Safe1, Index32}, no slow path.
+// warp-aggregated tickets, 64-bit entries {Cycle, Safe1, Index32}, no slow path.
 //
 // Kept from the reference: entry layout and INIT (glf_queue.hpp:66-90), modular
 // cycles (:96-110), the line-spreading slot permutation (:116-120), ring and
 // indirection layout (:126-138), enqueue/dequeue loops (:467-560), 64-bit payload
 // indirection (:566-582).
-// Changed for GB300: ring capacity and the permutation are runtime header fields;
+// Changed for GB300: the cycle tag is 16 bits by default (FQ_CYCLE_BITS; the
+// reference's knob, whose default of 8 bits wraps once an operation holds a ticket
+// 128 cycles behind the counters -- a stale entry then compares as current and a
+// value is lost or taken twice on rings of a few times the thread count); ring
+// capacity and the permutation are runtime header fields;
 // the enqueue CAS is tried first against the steady-state free slot, and a
 // dequeuer waits briefly for the enqueuer holding its ticket before marking the
 // slot (deq_wait);
@@ -23,7 +27,7 @@
 #define FQ_N 32768
 #endif
 #ifndef FQ_CYCLE_BITS
-#define FQ_CYCLE_BITS 8
+#define FQ_CYCLE_BITS 16
 #endif
 
 namespace gcq {
@@ -36,6 +40,7 @@ constexpr uint32_t BOT_C = 0xFFFFFFFFu;
 
 namespace ent {
 constexpr int CYCLE_SHIFT = 48, SAFE_SHIFT = 47;
+static_assert(FQ_CYCLE_BITS >= 4 && CYCLE_SHIFT + FQ_CYCLE_BITS <= 64, "the cycle tag must fit above bit 48");
 constexpr uint64_t SAFE_BIT = 1ULL << SAFE_SHIFT;
 constexpr uint64_t CONSUME_MASK = (uint64_t)BOT_C;
 constexpr uint64_t INIT = SAFE_BIT | (uint64_t)BOT;

@@ -3,13 +3,19 @@
 //
 // Kept from the reference (same bit layouts, same names):
 //   * global counter word {Counter, ThrIdx}          gwf_queue.hpp:31-92
-//   * 8-bit modular cycles                             gwf_queue.hpp:110-136
-//   * entry {Note8, Cycle8, Safe1, Enq1, Index32}      gwf_queue.hpp:149-189
+//   * modular cycle comparison                         gwf_queue.hpp:110-136
+//   * entry {Note, Cycle, Safe1, Enq1, Index32}        gwf_queue.hpp:149-189
 //   * local counter {cnt<<2 | INC | FIN}               gwf_queue.hpp:202-216
 //   * per-thread help request and phase-2 record       gwf_queue.hpp:242-288
 //   * ring {Tail, Head, Threshold, Entry[2N], Record}  gwf_queue.hpp:313-332
 //   * indirection {aq, fq, data[N]}                    gwf_queue.hpp:338-345
 // Changed for GB300:
+//   * Note and Cycle are 15 bits each by default (WF_CYCLE_BITS), not 8: they fill
+//     the 14 bits the reference's entry leaves zero (gwf_queue.hpp:140-146).  An
+//     8-bit tag wraps when an operation still holds a ticket 128 cycles behind the
+//     ring's counters (128 x 2N tickets), after which a stale entry compares as
+//     current; on rings of a few times the thread count that happens, and values
+//     are lost or taken twice.  WF_CYCLE_BITS=8 gives the reference's layout;
 //   * ring parameters (capacity, ThrIdx width, patience, help delay, slot remap) are
 //     runtime fields of the ring header, so one compiled kernel serves every
 //     capacity and thread count; the templates below fix them at compile time for
@@ -28,7 +34,7 @@
 #include "gcq_atomics.cuh"
 
 #ifndef WF_CYCLE_BITS
-#define WF_CYCLE_BITS 8
+#define WF_CYCLE_BITS 15
 #endif
 #ifndef WF_HELP_DELAY
 #define WF_HELP_DELAY 64
@@ -58,13 +64,18 @@ __host__ __device__ __forceinline__ int cycle_cmp(uint32_t a, uint32_t b) {
 }
 
 namespace entry {
-constexpr int NOTE_SHIFT = 56, CYCLE_SHIFT = 48, SAFE_SHIFT = 47, ENQ_SHIFT = 46;
+// Note and Cycle at the top of the word, Safe and Enq below them; 8 bits each
+// gives the reference's shifts 56 / 48 / 47 / 46.
+constexpr int NOTE_SHIFT = 64 - WF_CYCLE_BITS, CYCLE_SHIFT = 64 - 2 * WF_CYCLE_BITS;
+constexpr int SAFE_SHIFT = CYCLE_SHIFT - 1, ENQ_SHIFT = CYCLE_SHIFT - 2;
+static_assert(WF_CYCLE_BITS >= 4 && ENQ_SHIFT >= 32, "Note and Cycle must fit above the 32-bit index");
+constexpr uint32_t NOTE_NONE = CYCLE_MASK;  // Note = -1: no dequeuer has marked the slot
 constexpr uint64_t SAFE_BIT = 1ULL << SAFE_SHIFT;
 constexpr uint64_t ENQ_BIT = 1ULL << ENQ_SHIFT;
 constexpr uint32_t BOT = 0xFFFFFFFEu;    // empty
 constexpr uint32_t BOT_C = 0xFFFFFFFFu;  // consumed
 constexpr uint64_t CONSUME_MASK = ENQ_BIT | (uint64_t)BOT_C;
-constexpr uint64_t INIT = ((uint64_t)0xFF << NOTE_SHIFT) | SAFE_BIT | ENQ_BIT | BOT;
+constexpr uint64_t INIT = ((uint64_t)NOTE_NONE << NOTE_SHIFT) | SAFE_BIT | ENQ_BIT | BOT;
 __host__ __device__ __forceinline__ uint32_t note(uint64_t e) { return (uint32_t)(e >> NOTE_SHIFT) & CYCLE_MASK; }
 __host__ __device__ __forceinline__ uint32_t cycle(uint64_t e) { return (uint32_t)(e >> CYCLE_SHIFT) & CYCLE_MASK; }
 __host__ __device__ __forceinline__ bool safe(uint64_t e) { return (e >> SAFE_SHIFT) & 1; }

@@ -30,7 +30,7 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
     for (uint64_t s = gid; s < slots; s += nthreads) {
         const uint32_t pos = c.pos_of_slot((uint32_t)s);
         c.entry[s] = (full && pos < n)
-                         ? entry::pack(0xFF, c.cycle_of((uint64_t)slots + pos), true, true, pos)
+                         ? entry::pack(entry::NOTE_NONE, c.cycle_of((uint64_t)slots + pos), true, true, pos)
                          : entry::INIT;
         c.owner[s] = 0;
     }
@@ -128,8 +128,8 @@ __device__ inline uint64_t try_enq_at(ring* q, const cfg& c, uint32_t index, uin
     // value first.  A match means the enqueue conditions hold; a mismatch returns
     // the slot's current value, exactly what the load of gwf_ring.hpp:394 would
     // have read, so the code below continues from it.  Saves one L2 round trip.
-    uint64_t E = entry::pack(0xFF, tcyc - 1, true, true, BOT_C);
-    if (cas_upd_ord<Publish>(&c.entry[j], &E, entry::pack(0xFF, tcyc, true, true, index))) {
+    uint64_t E = entry::pack(entry::NOTE_NONE, tcyc - 1, true, true, BOT_C);
+    if (cas_upd_ord<Publish>(&c.entry[j], &E, entry::pack(entry::NOTE_NONE, tcyc, true, true, index))) {
         reset_threshold(&q->Threshold, c.threshold_max());
         return 0;
     }

@@ -24,7 +24,9 @@
 //
 // Where the reference's slow paths lose or duplicate values, the G-WFQ and YMC
 // restatements follow the published algorithms (each departure is marked where it
-// is made, and G-WFQ keeps flags that restore the reference's rules).
+// is made, and G-WFQ keeps flags that restore the reference's rules).  The G-WFQ
+// and G-LFQ cycle tags are 15 and 16 bits wide, as in the device code, instead of
+// the reference's 8; WF_CYCLE_BITS / FQ_CYCLE_BITS at compile time restore 8.
 //
 // Runners at the end drive them like the reference harnesses:
 //   history      correctness/history.cpp:188-227 with the logical clock of
@@ -63,12 +65,20 @@ static inline void cpu_relax() { std::this_thread::yield(); }
 // =============================================================================
 namespace gwf {
 
-constexpr u32 CYCLE_MASK = 0xFF, HALF_CYCLE = 0x80;
-constexpr int NOTE_SHIFT = 56, CYCLE_SHIFT = 48, SAFE_SHIFT = 47, ENQ_SHIFT = 46;
+// Note and Cycle take WF_CYCLE_BITS each at the top of the entry, as in the device
+// code; 8 (-DWF_CYCLE_BITS=8) gives gwf_queue.hpp's layout (:110-116, :140-160),
+// whose tag wraps when an operation holds a ticket 128 cycles behind the counters.
+#ifndef WF_CYCLE_BITS
+#define WF_CYCLE_BITS 15
+#endif
+constexpr u32 CYCLE_MASK = (1u << WF_CYCLE_BITS) - 1, HALF_CYCLE = 1u << (WF_CYCLE_BITS - 1);
+constexpr int NOTE_SHIFT = 64 - WF_CYCLE_BITS, CYCLE_SHIFT = 64 - 2 * WF_CYCLE_BITS;
+constexpr int SAFE_SHIFT = CYCLE_SHIFT - 1, ENQ_SHIFT = CYCLE_SHIFT - 2;
+static_assert(ENQ_SHIFT >= 32, "Note and Cycle must fit above the 32-bit index");
 constexpr u64 SAFE_BIT = 1ULL << SAFE_SHIFT, ENQ_BIT = 1ULL << ENQ_SHIFT;
 constexpr u32 BOT = 0xFFFFFFFEu, BOT_C = 0xFFFFFFFFu;
 constexpr u64 CONSUME_MASK = ENQ_BIT | (u64)BOT_C;
-constexpr u64 INIT = (0xFFULL << NOTE_SHIFT) | SAFE_BIT | ENQ_BIT | BOT;
+constexpr u64 INIT = ((u64)CYCLE_MASK << NOTE_SHIFT) | SAFE_BIT | ENQ_BIT | BOT;
 constexpr u64 FIN = 1, INC = 2, CNT_MASK = ~3ULL;
 
 static inline u32 note(u64 e) { return (u32)((e >> NOTE_SHIFT) & CYCLE_MASK); }
@@ -155,7 +165,7 @@ struct Ring {
         if (full) {  // gwf_ring.hpp:286-297
             for (u32 i = 0; i < n; ++i) {
                 u64 t = (u64)slots + i;
-                Entry[slot_of(t)].store(pack(0xFF, cycle_of(t), true, true, i));
+                Entry[slot_of(t)].store(pack(CYCLE_MASK, cycle_of(t), true, true, i));
             }
             Tail = packg((u64)slots + n, (u32)null_tid);
             Threshold = thr_max();
@@ -518,7 +528,13 @@ struct Mpmc {
 // =============================================================================
 namespace glf {
 
-constexpr u32 CYCLE_MASK = 0xFF, HALF = 0x80;
+// The cycle tag takes FQ_CYCLE_BITS above bit 48, as in the device code; 8 gives
+// glf_queue.hpp's default (:36-47).
+#ifndef FQ_CYCLE_BITS
+#define FQ_CYCLE_BITS 16
+#endif
+constexpr u32 CYCLE_MASK = (1u << FQ_CYCLE_BITS) - 1, HALF = 1u << (FQ_CYCLE_BITS - 1);
+static_assert(48 + FQ_CYCLE_BITS <= 64, "the cycle tag must fit above bit 48");
 constexpr u32 BOT = 0xFFFFFFFEu, BOT_C = 0xFFFFFFFFu;
 constexpr u64 SAFE_BIT = 1ULL << 47;
 constexpr u64 INIT = SAFE_BIT | BOT;
@@ -539,6 +555,7 @@ struct Ring {
     u32 cycle_of(u64 t) const { return (u32)((t / slots) & CYCLE_MASK); }
     u32 remap(u64 t) const {
         u32 p = (u32)(t & (slots - 1));
+        if (slots <= PER_LINE) return p;  // one line: glf_queue.hpp:116-120 would send every ticket to slot 0
         return (p & (PER_LINE - 1)) * (slots / PER_LINE) + p / PER_LINE;
     }
     int32_t thr_max() const { return 3 * (int32_t)n - 1; }
@@ -1737,6 +1754,68 @@ int oracle_gwf_device_model_stress(uint32_t threads, uint32_t ops, uint32_t n, u
         u64 o;
         for (u32 misses = 0, k2 = 0; k2 < threads * ops + 64 && misses < 64; ++k2) {
             if (d.dequeue_ptr(&o, 0, x)) take(o);
+            else ++misses;
+        }
+        for (size_t i = 0; i < counts.size(); ++i) ok = ok && counts[i] == in[i];
+        failed += ok ? 0 : 1;
+    }
+    return failed;
+}
+
+// Exactly-once stress of the ports' MPMC queues as the reference composes them
+// (gwf_ring.hpp:1362-1380, glf_queue.hpp:566-582): kind 0 G-WFQ with the given
+// patiences and help delay, kind 1 G-LFQ (which has none); `threads` threads each
+// run `ops` enqueue-then-dequeue pairs on an n-entry queue, which is then drained.
+// Returns how many of `runs` runs lost, duplicated or invented a value.
+int oracle_port_mpmc_stress(int kind, uint32_t threads, uint32_t ops, uint32_t n, uint32_t enq_patience,
+                            uint32_t deq_patience, uint32_t help_delay, uint32_t runs) {
+    if ((kind != 0 && kind != 1) || threads < 1 || threads > 64 || ops == 0 || ops > 4096 || n < 2 ||
+        (n & (n - 1)) || n < threads || help_delay == 0 || runs == 0)
+        return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        gwf::Mpmc wq;
+        glf::Mpmc lq;
+        if (kind == 0) {
+            gwf::Knobs k;
+            k.enq_patience = (int)enq_patience;
+            k.deq_patience = (int)deq_patience;
+            k.help_delay = (int)help_delay;
+            wq.init(n, threads, bits_for(threads), k);
+        } else {
+            lq.init(n);
+        }
+        auto enqueue = [&](u64 v, u32 w) { return kind == 0 ? wq.enqueue(v, w) : lq.enqueue(v); };
+        auto dequeue = [&](u64* o, u32 w) { return kind == 0 ? wq.dequeue(o, w) : lq.dequeue(o); };
+        std::vector<std::vector<u64>> got(threads), put(threads);
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                for (u32 i = 0; i < ops; ++i) {
+                    const u64 v = 1000 + (u64)w * ops + i;
+                    u64 o;
+                    if (enqueue(v, w)) put[w].push_back(v);
+                    if (dequeue(&o, w)) got[w].push_back(o);
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts((size_t)threads * ops, 0), in((size_t)threads * ops, 0);
+        for (auto& p : put)
+            for (u64 v : p) in[v - 1000] = 1;
+        bool ok = true;
+        auto take = [&](u64 v) {
+            if (v < 1000 || v - 1000 >= (u64)threads * ops || !in[v - 1000]) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u64 v : g) take(v);
+        u64 o;
+        for (u32 misses = 0, k2 = 0; k2 < threads * ops + 64 && misses < 64; ++k2) {
+            if (dequeue(&o, 0)) take(o);
             else ++misses;
         }
         for (size_t i = 0; i < counts.size(); ++i) ok = ok && counts[i] == in[i];

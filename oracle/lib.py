@@ -89,6 +89,8 @@ _EXTRA = [
                                  C.c_uint32, C.c_int], C.c_int),
     ("oracle_gwf_device_model_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                         C.c_int, C.c_int, C.c_int, C.c_uint32], C.c_int),
+    ("oracle_port_mpmc_stress", [C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                 C.c_uint32], C.c_int),
 ]
 
 

@@ -134,3 +134,42 @@ def test_gwf_split_small_ring_exactly_once(oracle_lib, P, C, K, n):
     ticket the owner returned empty while that helper later claimed an element for
     it (0.2-0.35 % of runs lost a value)."""
     assert oracle_lib.lib().oracle_gwf_split_stress(P, C, K, n, 2, 2, 1, 400, 0) == 0
+
+
+# (kind, threads, ops, n, enq_patience, deq_patience, help_delay, runs); kind 0 is
+# G-WFQ, 1 is G-LFQ (no patience or helping).  With 8-bit cycle tags the G-WFQ cases
+# lost values in 0.5-60 % of runs and the first two G-LFQ cases in 0.6-30 %.  The last
+# is a ring of one 8-entry line, which glf_queue.hpp:116-120's permutation maps
+# entirely to slot 0 (the port keeps such rings unpermuted, as the device code does).
+_TAG_CASES = [(0, 8, 512, 8, 2, 2, 1, 300), (0, 4, 1024, 8, 3, 8, 8, 200), (0, 2, 2048, 4, 3, 4, 1, 200),
+              (1, 16, 2048, 16, 1, 1, 1, 300), (1, 8, 4096, 8, 1, 1, 1, 300), (1, 2, 4096, 2, 1, 1, 1, 200)]
+
+
+@pytest.mark.parametrize("kind, threads, ops, n, pe, pd, hd, runs", _TAG_CASES)
+def test_wide_cycle_tags_exactly_once(oracle_lib, kind, threads, ops, n, pe, pd, hd, runs):
+    """The MPMC queues on rings of 2-16 entries, where an operation can hold its
+    ticket while the ring's counters run 128 cycles ahead: with the 15-bit (G-WFQ)
+    and 16-bit (G-LFQ) cycle tags of the device code every value comes out exactly
+    once."""
+    assert oracle_lib.lib().oracle_port_mpmc_stress(kind, threads, ops, n, pe, pd, hd, runs) == 0
+
+
+def test_eight_bit_cycle_tags_lose_values(tmp_path):
+    """The control: the same ports built with the reference's 8-bit tags
+    (gwf_queue.hpp:109-116, glf_queue.hpp:36-47) lose or duplicate values on those
+    rings, because a tag 128 cycles stale compares as current.  Run in a child
+    process with a time limit, since G-LFQ's enqueue retries without bound."""
+    import os
+    import subprocess
+    import sys
+    src = os.path.join(os.path.dirname(__file__), "..", "oracle", "cpu_queues.cpp")
+    lib = str(tmp_path / "libq8.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-shared", "-DWF_CYCLE_BITS=8",
+                    "-DFQ_CYCLE_BITS=8", src, "-o", lib], check=True)
+    prog = ("import ctypes as C, sys\n"
+            "f = C.CDLL(sys.argv[1]).oracle_port_mpmc_stress\n"
+            "f.argtypes = [C.c_int] + [C.c_uint32] * 7\n"
+            "print(f(0, 8, 512, 8, 2, 2, 1, 300), f(1, 16, 2048, 16, 1, 1, 1, 300))\n")
+    out = subprocess.run([sys.executable, "-c", prog, lib], capture_output=True, text=True, timeout=120, check=True)
+    wfq_failed, lfq_failed = map(int, out.stdout.split())
+    assert wfq_failed > 0 and lfq_failed > 0, (wfq_failed, lfq_failed)
