@@ -261,6 +261,11 @@ struct wf_t {
     static_assert(Config::MAX_THREADS <= N, "wf requires k <= n");
     static_assert(gcq::gwf::CYCLE_RANGE > 2u * (WF_HELP_DELAY * (uint64_t)Config::MAX_THREADS / (2 * N) + 3),
                   "cycle bits insufficient for this thread/buffer configuration");
+    // Patience 1 would start the slow path without a failed ticket of its own (at
+    // counter 0, the same start for every request of a thread); the library's
+    // gcq_create refuses it as well.
+    static_assert(WF_ENQ_PATIENCE >= 2 && WF_DEQ_PATIENCE >= 2 && WF_HELP_DELAY >= 1,
+                  "WF_ENQ_PATIENCE and WF_DEQ_PATIENCE must be at least 2, WF_HELP_DELAY at least 1");
     gcq::gwf::ring hdr;
     gcq::u32a err;
     unsigned long long Entry[SLOTS];

@@ -54,7 +54,14 @@ __device__ inline void init_slice(ring* q, bool full, uint64_t gid, uint64_t nth
 // ------------------------------------------------------------------ consume etc.
 // finalize_request, gwf_ring.hpp:309-328: set FIN on the slow-path enqueuer whose
 // localTail holds ticket h.  The slot's owner entry names that record; the scan of
-// all records remains as the fallback when it no longer matches.
+// all records remains as the fallback when it no longer matches.  A localTail whose
+// counter is h with INC set belongs to a request that tried to claim h in the
+// cooperative fetch-and-add and lost; the holder has h without INC from before it
+// produced the entry until FIN.  The reference's scan stops at the first counter
+// match (:322-325): when that is such a loser, the holder never gets FIN while its
+// producer is delayed, its helpers take the consumed slot as produced until the slot
+// is reused a cycle later, then move on and produce the index a second time.  Both
+// lookups here match h without INC.
 __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j, uint32_t tid) {
     GCQ_STAT(c, stat::FINALIZE);
     const uint64_t h_local = h_raw << 2;
@@ -64,7 +71,7 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j
     const uint32_t own = ld_rlx(&c.owner[j]);
     if (own != 0 && own <= c.max_threads) {
         const uint64_t lt = ld_acq(&c.rec[own - 1].localTail);
-        if ((lt & local::CNT_MASK) == h_local) {
+        if ((lt & ~local::FIN) == h_local) {
             cas(&c.rec[own - 1].localTail, h_local, h_local | local::FIN);
             return;
         }
@@ -73,7 +80,7 @@ __device__ inline void finalize_request(const cfg& c, uint64_t h_raw, uint32_t j
     uint32_t i = (tid + 1 == c.max_threads) ? 0 : tid + 1;
     while (i != tid) {
         const uint64_t lt = ld_acq(&c.rec[i].localTail);
-        if ((lt & local::CNT_MASK) == h_local) {
+        if ((lt & ~local::FIN) == h_local) {
             cas(&c.rec[i].localTail, h_local, h_local | local::FIN);
             return;
         }

@@ -131,6 +131,9 @@ struct Ring {
     // true: gwf_ring.hpp:729-731, 763-766 verbatim (a slow dequeue attempt reports
     // the request done whatever its FIN CAS found); false: done only once FIN is set
     bool reference_finish_rule = false;
+    // true: gwf_ring.hpp:316-326 verbatim (finalize_request stops at the first
+    // record whose localTail counter is h, INC or not); false: the holder of h only
+    bool reference_finalize_scan = false;
     std::unique_ptr<std::atomic<u64>[]> Entry;
     std::unique_ptr<Rec[]> Record;
 
@@ -173,12 +176,20 @@ struct Ring {
     }
 
     // ---- consume / finalize / catchup --------------------------------------
+    // Sets FIN on the request that holds ticket h.  A localTail whose counter is h
+    // with INC set belongs to a request that tried to claim h in the cooperative
+    // fetch-and-add and lost (its next attempt moves it on); the holder's localTail
+    // is h without INC from before it produced the entry until FIN.  The reference
+    // stops at the first counter match: when that is a loser, the holder never gets
+    // FIN while its producer is delayed, its helpers take the consumed slot as
+    // produced until the slot is reused a cycle later, then move on and produce the
+    // index a second time.  So the scan passes over INC matches.
     void finalize_request(u64 h_raw, u32 me) {
         u64 hl = h_raw << 2;
         u32 i = (me + 1) % max_threads;
         while (i != me) {
             u64 lt = Record[i].localTail.load();
-            if ((lt & CNT_MASK) == hl) {
+            if (reference_finalize_scan ? (lt & CNT_MASK) == hl : (lt & ~FIN) == hl) {
                 u64 e = hl;
                 Record[i].localTail.compare_exchange_strong(e, hl | FIN);
                 return;
@@ -1195,6 +1206,120 @@ struct Queue {
 };
 }  // namespace gwfmodel
 
+// The device G-LFQ ring operations (a model of the device code, not of the
+// reference): slots in ticket order (the device's default; the reference spreads
+// them over lines), the enqueue CAS tried first against the steady-state free
+// slot, a bounded wait for the enqueuer holding the dequeuer's ticket before the
+// slot is marked (deq_wait), and the empty exit before a retry ticket.
+namespace glfmodel {
+using namespace glf;
+struct Ring {
+    alignas(128) std::atomic<u64> Tail{0};
+    alignas(128) std::atomic<u64> Head{0};
+    alignas(128) std::atomic<int32_t> Threshold{-1};
+    u32 n = 0, slots = 0, deq_wait = 0;
+    std::unique_ptr<std::atomic<u64>[]> Entry;
+    u32 cycle_of(u64 t) const { return (u32)((t / slots) & CYCLE_MASK); }
+    u32 slot_of(u64 t) const { return (u32)(t & (slots - 1)); }
+    int32_t thr_max() const { return 3 * (int32_t)n - 1; }
+    void init(u32 n_, bool full, u32 wait) {
+        n = n_; slots = 2 * n; deq_wait = wait;
+        Entry.reset(new std::atomic<u64>[slots]);
+        for (u32 i = 0; i < slots; ++i) Entry[i].store(INIT);
+        Head = slots;
+        Tail = full ? (u64)slots + n : (u64)slots;
+        Threshold = full ? thr_max() : -1;
+        if (full)
+            for (u32 i = 0; i < n; ++i) Entry[slot_of((u64)slots + i)].store(pack(cycle_of((u64)slots + i), true, i));
+    }
+    void catchup(u64 tail, u64 head) {
+        for (int i = 0; i < 32; ++i) {
+            if (Tail.compare_exchange_strong(tail, head)) break;
+            head = Head.load();
+            tail = Tail.load();
+            if (tail >= head) break;
+        }
+    }
+    void enqueue(u32 index) {
+        for (;;) {
+            const u64 T = Tail.fetch_add(1);
+            const u32 tc = cycle_of(T), j = slot_of(T);
+            u64 E = pack(tc - 1, true, BOT_C);
+            if (Entry[j].compare_exchange_strong(E, pack(tc, true, index))) {
+                if (Threshold.load() != thr_max()) Threshold.exchange(thr_max());
+                return;
+            }
+            for (;;) {
+                const u32 ec = cyc(E), ei = idx(E);
+                if (ccmp(ec, tc) >= 0 || ei < BOT) break;
+                if (!safe(E) && Head.load() > T) break;
+                if (!Entry[j].compare_exchange_strong(E, pack(tc, true, index))) continue;
+                if (Threshold.load() != thr_max()) Threshold.exchange(thr_max());
+                return;
+            }
+        }
+    }
+    u32 dequeue() {
+        if (Threshold.load() < 0) return BOT;
+        for (;;) {
+            const u64 H = Head.fetch_add(1);
+            const u32 hc = cycle_of(H), j = slot_of(H);
+            u64 E = Entry[j].load();
+            for (u32 w = 0; w < deq_wait && ccmp(cyc(E), hc) < 0 && idx(E) >= BOT; ++w) {
+                cpu_relax();
+                E = Entry[j].load();
+            }
+            for (;;) {
+                const u32 ec = cyc(E), ei = idx(E);
+                if (ccmp(ec, hc) == 0 && ei < BOT) {
+                    Entry[j].fetch_or((u64)BOT_C);
+                    return ei;
+                }
+                if (ccmp(ec, hc) >= 0) break;
+                const u64 nw = ei >= BOT ? pack(hc, safe(E), BOT) : pack(ec, false, ei);
+                if (Entry[j].compare_exchange_strong(E, nw)) break;
+            }
+            const u64 T = Tail.load();
+            if (T <= H + 1) {
+                catchup(T, H + 1);
+                Threshold.fetch_sub(1);
+                return BOT;
+            }
+            if (Threshold.fetch_sub(1) <= 0) return BOT;
+            const u64 h = Head.load(), t = Tail.load();
+            if (t <= h) {
+                if (t < h) catchup(t, h);
+                return BOT;
+            }
+        }
+    }
+};
+struct Queue {
+    Ring aq, fq;
+    std::unique_ptr<std::atomic<u64>[]> data;
+    void init(u32 n, u32 deq_wait) {
+        aq.init(n, false, deq_wait);
+        fq.init(n, true, deq_wait);
+        data.reset(new std::atomic<u64>[n]);
+        for (u32 i = 0; i < n; ++i) data[i].store(0, std::memory_order_relaxed);
+    }
+    bool enqueue_ptr(u64 v) {
+        const u32 i = fq.dequeue();
+        if (i == BOT) return false;
+        data[i].store(v, std::memory_order_relaxed);
+        aq.enqueue(i);
+        return true;
+    }
+    bool dequeue_ptr(u64* out) {
+        const u32 i = aq.dequeue();
+        if (i == BOT) return false;
+        *out = data[i].load(std::memory_order_relaxed);
+        fq.enqueue(i);
+        return true;
+    }
+};
+}  // namespace glfmodel
+
 }  // namespace
 
 extern "C" {
@@ -1448,6 +1573,30 @@ int oracle_gwf_slow_passed_slot(int reference_rule, uint32_t* deq_out) {
     return done_at_T ? 1 : 0;
 }
 
+// finalize_request with a losing claimant, deterministically: thread 2's request
+// holds Tail ticket T and its producer has written index 5 there with Enq = 0 but
+// not yet set FIN (it is delayed); thread 1's request tried to claim T in the
+// cooperative fetch-and-add and lost, so its localTail reads T | INC.  Thread 0
+// dequeues ticket T and finalizes.  out[0] and out[1] receive the two localTails
+// afterwards; returns the dequeued index.  reference_scan = 1 runs the scan of
+// gwf_ring.hpp:316-326.
+int oracle_gwf_finalize_loser(int reference_scan, uint64_t* out) {
+    gwf::Ring q;
+    q.init(8, 4, 2, gwf::Knobs());
+    q.reference_finalize_scan = reference_scan != 0;
+    const u64 T = q.cnt_of(q.Tail.fetch_add(q.cinc));
+    q.Record[1].localTail.store((T << 2) | gwf::INC);
+    q.Record[2].localTail.store(T << 2);
+    const u32 j = q.slot_of(T);
+    const u64 E = q.Entry[j].load();
+    q.Entry[j].store(gwf::pack(gwf::note(E), q.cycle_of(T), true, false, 5));
+    u32 got = gwf::BOT;
+    if (q.try_deq(&got, 0) != 0) return -1;
+    out[0] = q.Record[1].localTail.load();
+    out[1] = q.Record[2].localTail.load();
+    return (int)got;
+}
+
 // Host fault injection for the wait-free helping of G-WFQ (gwf_ring.hpp:808-861,
 // restated above): thread 0 takes a Tail ticket, publishes a slow-path enqueue
 // request for index `stalled_index` and then stalls -- it makes no further step --
@@ -1543,10 +1692,10 @@ int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_del
 // run `ops` enqueue/dequeue pairs of their own values with the given patiences
 // (1: every operation starts on the slow path; 2: after one failed fast-path
 // attempt) and help delay, then the queue is drained.  Returns how many of `runs`
-// runs lost or duplicated a value.  reference_help = 1 runs the phase-2 help of
-// gwf_ring.hpp:548-590 verbatim.
+// runs lost or duplicated a value.  reference_rules bit 0 runs the phase-2 help of
+// gwf_ring.hpp:548-590 verbatim, bit 1 the finalize_request scan of :316-326.
 int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience, uint32_t deq_patience,
-                           uint32_t help_delay, uint32_t runs, int reference_help) {
+                           uint32_t help_delay, uint32_t runs, int reference_rules) {
     if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || help_delay == 0 || runs == 0) return -1;
     int failed = 0;
     for (uint32_t run = 0; run < runs; ++run) {
@@ -1556,7 +1705,8 @@ int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience
         kn.enq_patience = (int)enq_patience;
         kn.deq_patience = (int)deq_patience;
         q.init(1024, threads, bits_for(threads), kn);
-        q.reference_phase2_help = reference_help != 0;
+        q.reference_phase2_help = (reference_rules & 1) != 0;
+        q.reference_finalize_scan = (reference_rules & 2) != 0;
         std::vector<std::vector<u32>> got(threads);
         std::vector<std::thread> ths;
         std::atomic<int> ready{0};
@@ -1816,6 +1966,59 @@ int oracle_port_mpmc_stress(int kind, uint32_t threads, uint32_t ops, uint32_t n
         u64 o;
         for (u32 misses = 0, k2 = 0; k2 < threads * ops + 64 && misses < 64; ++k2) {
             if (dequeue(&o, 0)) take(o);
+            else ++misses;
+        }
+        for (size_t i = 0; i < counts.size(); ++i) ok = ok && counts[i] == in[i];
+        failed += ok ? 0 : 1;
+    }
+    return failed;
+}
+
+// Exactly-once stress of the G-LFQ device-path model (glfmodel above), driven as
+// oracle_gwf_device_model_stress drives G-WFQ's: balanced (mode 0) or split
+// (mode 1, the first producer_percent % of threads enqueue) on an n-entry queue,
+// then drained; deq_wait is the dequeuer's bounded wait.  Returns how many of
+// `runs` runs lost, duplicated or invented a value.
+int oracle_glf_device_model_stress(uint32_t threads, uint32_t ops, uint32_t n, int mode, int producer_percent,
+                                   uint32_t deq_wait, uint32_t runs) {
+    if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || n < 2 || (n & (n - 1)) || runs == 0)
+        return -1;
+    int failed = 0;
+    for (uint32_t run = 0; run < runs; ++run) {
+        glfmodel::Queue d;
+        d.init(n, deq_wait);
+        std::vector<std::vector<u64>> got(threads), put(threads);
+        std::vector<std::thread> ths;
+        std::atomic<int> ready{0};
+        for (u32 w = 0; w < threads; ++w) {
+            ths.emplace_back([&, w]() {
+                ready.fetch_add(1);
+                while (ready.load() < (int)threads) cpu_relax();
+                const bool producer = (u64)w * 100 / threads < (u64)producer_percent;
+                for (u32 i = 0; i < ops; ++i) {
+                    const u64 v = 1000 + (u64)w * ops + i;
+                    u64 o;
+                    if (mode == 0 || producer)
+                        if (d.enqueue_ptr(v)) put[w].push_back(v);
+                    if (mode == 0 || !producer)
+                        if (d.dequeue_ptr(&o)) got[w].push_back(o);
+                }
+            });
+        }
+        for (auto& th : ths) th.join();
+        std::vector<u32> counts((size_t)threads * ops, 0), in((size_t)threads * ops, 0);
+        for (auto& p : put)
+            for (u64 v : p) in[v - 1000] = 1;
+        bool ok = true;
+        auto take = [&](u64 v) {
+            if (v < 1000 || v - 1000 >= (u64)threads * ops || !in[v - 1000]) ok = false;
+            else ++counts[v - 1000];
+        };
+        for (auto& g : got)
+            for (u64 v : g) take(v);
+        u64 o;
+        for (u32 misses = 0, k2 = 0; k2 < threads * ops + 64 && misses < 64; ++k2) {
+            if (d.dequeue_ptr(&o)) take(o);
             else ++misses;
         }
         for (size_t i = 0; i < counts.size(); ++i) ok = ok && counts[i] == in[i];

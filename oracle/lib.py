@@ -81,6 +81,7 @@ _EXTRA = [
      C.c_int64),
     ("oracle_levels_checksum", [C.c_int32, C.c_void_p], C.c_uint64),
     ("oracle_gwf_slow_passed_slot", [C.c_int, C.c_void_p], C.c_int),
+    ("oracle_gwf_finalize_loser", [C.c_int, C.c_void_p], C.c_int),
     ("oracle_gwf_stalled_helping", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p], C.c_int),
     ("oracle_gwf_slow_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int],
      C.c_int),
@@ -91,6 +92,8 @@ _EXTRA = [
                                         C.c_int, C.c_int, C.c_int, C.c_uint32], C.c_int),
     ("oracle_port_mpmc_stress", [C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32], C.c_int),
+    ("oracle_glf_device_model_stress", [C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_uint32, C.c_uint32],
+     C.c_int),
 ]
 
 

@@ -173,3 +173,34 @@ def test_eight_bit_cycle_tags_lose_values(tmp_path):
     out = subprocess.run([sys.executable, "-c", prog, lib], capture_output=True, text=True, timeout=120, check=True)
     wfq_failed, lfq_failed = map(int, out.stdout.split())
     assert wfq_failed > 0 and lfq_failed > 0, (wfq_failed, lfq_failed)
+
+
+@pytest.mark.parametrize("threads, ops, n, mode, pct, deq_wait",
+                         [(8, 512, 8, 0, 50, 0), (8, 512, 8, 0, 50, 8), (16, 2048, 16, 0, 50, 0),
+                          (16, 256, 16, 1, 75, 4), (16, 256, 16, 1, 25, 0), (32, 128, 32, 1, 50, 2)])
+def test_glf_device_path_model_exactly_once(oracle_lib, threads, ops, n, mode, pct, deq_wait):
+    """The device G-LFQ additions restated over CPU rings (slots in ticket order, the
+    enqueue CAS tried against the steady-state free slot first, the dequeuer's
+    bounded wait for its ticket's enqueuer, the empty exit before a retry ticket):
+    every value comes out exactly once, balanced and split, on rings of 8-32
+    entries.  (With 8-bit cycle tags the third configuration loses values in about
+    a quarter of its runs.)"""
+    assert oracle_lib.lib().oracle_glf_device_model_stress(threads, ops, n, mode, pct, deq_wait, 200) == 0
+
+
+def test_gwf_finalize_passes_losing_claimant(oracle_lib):
+    """A consumed Enq = 0 entry at ticket T sets FIN on the request that holds T,
+    not on a request whose localTail reads T | INC because it tried to claim T in
+    the cooperative fetch-and-add and lost.  gwf_ring.hpp:316-326 stops at the first
+    record whose counter is T: the loser's CAS fails and the holder is left without
+    FIN.  In the stress of the port (16 threads, enqueues on the slow path, patience
+    1) that produced a value twice in 4-7 of 3000 runs: the holder's helpers took
+    the consumed slot as produced until it was reused a cycle later, then moved on
+    and produced the index again."""
+    import numpy as np
+    T = 16 << 2  # first ticket of an 8-entry ring, as a localTail value
+    out = np.zeros(2, np.uint64)
+    assert oracle_lib.lib().oracle_gwf_finalize_loser(0, out.ctypes.data) == 5
+    assert (int(out[0]), int(out[1])) == (T | 2, T | 1)      # loser untouched, holder FIN
+    assert oracle_lib.lib().oracle_gwf_finalize_loser(1, out.ctypes.data) == 5
+    assert (int(out[0]), int(out[1])) == (T | 2, T)          # the reference's scan
