@@ -134,6 +134,9 @@ struct Ring {
     // true: gwf_ring.hpp:316-326 verbatim (finalize_request stops at the first
     // record whose localTail counter is h, INC or not); false: the holder of h only
     bool reference_finalize_scan = false;
+    // true: gwf_ring.hpp:1242-1251 verbatim (with patience 1 the slow path starts
+    // at counter 0); false: it starts from a Tail ticket of its own
+    bool reference_patience1_start = false;
     std::unique_ptr<std::atomic<u64>[]> Entry;
     std::unique_ptr<Rec[]> Record;
 
@@ -461,6 +464,15 @@ struct Ring {
             tail = try_enq(index);
             if (tail == 0) return;
         }
+        // With patience 1 no fast-path attempt leaves a failed ticket, and the
+        // reference starts the slow path at counter 0 -- the start of every request
+        // of this thread.  A helper of the thread's previous request whose view is
+        // still 0 can then CAS the new request's localTail to a count that request
+        // already used, and once INC is cleared the new request holds a spent
+        // ticket: it takes the consumed slot as produced and its value is lost.  A
+        // ticket taken here, and left unused like a failed attempt, makes the start
+        // unique.  (The library refuses patience below 2.)
+        if (tail == 0 && !reference_patience1_start) tail = cnt_of(Tail.fetch_add(cinc));
         Rec& r = Record[me];
         u32 seq = r.seq1.load();
         r.localTail.store(tail << 2);
@@ -1693,7 +1705,8 @@ int oracle_gwf_stalled_helping(uint32_t threads, uint32_t ops, uint32_t help_del
 // (1: every operation starts on the slow path; 2: after one failed fast-path
 // attempt) and help delay, then the queue is drained.  Returns how many of `runs`
 // runs lost or duplicated a value.  reference_rules bit 0 runs the phase-2 help of
-// gwf_ring.hpp:548-590 verbatim, bit 1 the finalize_request scan of :316-326.
+// gwf_ring.hpp:548-590 verbatim, bit 1 the finalize_request scan of :316-326, bit 2
+// the patience-1 slow-path start of :1242-1251.
 int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience, uint32_t deq_patience,
                            uint32_t help_delay, uint32_t runs, int reference_rules) {
     if (threads < 1 || threads > 64 || ops == 0 || ops > 4096 || help_delay == 0 || runs == 0) return -1;
@@ -1707,6 +1720,7 @@ int oracle_gwf_slow_stress(uint32_t threads, uint32_t ops, uint32_t enq_patience
         q.init(1024, threads, bits_for(threads), kn);
         q.reference_phase2_help = (reference_rules & 1) != 0;
         q.reference_finalize_scan = (reference_rules & 2) != 0;
+        q.reference_patience1_start = (reference_rules & 4) != 0;
         std::vector<std::vector<u32>> got(threads);
         std::vector<std::thread> ths;
         std::atomic<int> ready{0};
